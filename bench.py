@@ -1,0 +1,351 @@
+"""Throughput benchmark of the fused GB300 MHD step.
+
+Workload (the configuration the headline metric is quoted on): 2D
+Kelvin-Helmholtz shear layer, 4096 x 2048 interior cells, x periodic, y
+zero-gradient walls, HLLD + minmod + GLM + TVD-RK2, CFL 0.4, FP64.  One step =
+one full TVD-RK2 step (two fused stage kernels) over the whole grid.  The
+state (605 MB) is larger than L2 (129 MB), so no L2 flush is needed between
+steps.  Synthetic seeded initial data (no external dataset exists).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  --impl reference times the CPU restatement of
+the reference's serial Fortran path (the oracle port, OpenMP over all host
+cores) on the same workload.  Multi-GPU runs are independent replicas, one per
+GPU ("replicas only": the path has no exchange once one GPU holds a grid).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX, NY = 4096, 2048
+WORKLOAD = "kh2d_4096x2048_hlld_minmod_glm_tvdrk2"
+# Algorithmic cost of one 2D cell-update (both RK stages, GLM, CFL) is read
+# from profiles/flops_kh2d.txt (flop-counting build of the oracle on this
+# workload: add/sub/mul/div/sqrt/exp = 1 flop, min/max/abs/sign/compare = 0).
+BYTES_PER_CELL_UPDATE_2D = 45 * 8  # stage 1: read U, write U1; stage 2: read U, U1, write U
+
+
+def _load_flops():
+    p = os.path.join(ROOT, "profiles", "flops_kh2d.txt")
+    if os.path.exists(p):
+        m = re.search(r"flops_per_cell_update:\s*([0-9.]+)", open(p).read())
+        if m:
+            return float(m.group(1))
+    return 2100.0  # estimate until the counting build has run
+
+
+def _load_traffic(name: str):
+    p = os.path.join(ROOT, "profiles", name)
+    if os.path.exists(p):
+        m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(p).read())
+        if m:
+            return float(m.group(1))
+    return None
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_id: str | None):
+        self.dev = device_id
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+        if self.dev:
+            cmd += ["-i", self.dev]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def aggregate(per_rank_seconds: list[float], cells_per_rank: int, steps: int) -> tuple[float, float]:
+    """Whole-job throughput of independent replicas: all ranks' cell-updates
+    divided by the slowest rank's time (max over ranks)."""
+    t = max(per_rank_seconds)
+    return len(per_rank_seconds) * cells_per_rank * steps / t, t
+
+
+def cpu_baseline(steps_budget_s: float = 12.0, omp: bool = True, nx: int = NX, ny: int = NY):
+    """Oracle (C restatement of the reference's serial path) on the host cores,
+    same KH workload, bounded to about `steps_budget_s` of CPU time."""
+    from oracle import oracle
+    from openmhd_gb300 import kelvin_helmholtz
+
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    cfg, model = kelvin_helmholtz(nx, ny, precision="fp64")
+    g = oracle.Grid.from_solver_config(cfg, omp=omp)
+    g.model(model.kind, amp=model.amp, bx0=model.bx0, pert=model.pert, seed=model.seed)
+    g.step(1)  # warm-up (page-in)
+    done, t0 = 0, time.perf_counter()
+    while True:
+        g.step(1)
+        done += 1
+        el = time.perf_counter() - t0
+        if el >= steps_budget_s or done >= 50:
+            break
+    cells = (nx * ny)
+    return {"value": cells * done / el, "unit": "cell-updates/s", "cores": int(os.environ["OMP_NUM_THREADS"]) if omp else 1,
+            "kind": "port", "sample": f"{done} steps of KH {nx}x{ny} after 1 warm-up step ({el:.1f} s)"}, el / done
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    base, _ = cpu_baseline(steps_budget_s=min(60.0, max(8.0, 4.0 * args.steps)))
+    line = {
+        "impl": "reference", "metric": "cell-updates/s", "value": base["value"], "unit": "cell-updates/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "precision": "fp64",
+                   "note": "reference is Fortran (no compiler here or on the box): C restatement, OpenMP"},
+        "cpu_baseline": base,
+        "e2e": {"value": base["value"], "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from openmhd_gb300 import Solver, kelvin_helmholtz
+    from openmhd_gb300 import _lib
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.cuda.current_device()
+    props = torch.cuda.get_device_properties(dev)
+    uuid = None
+    try:
+        uuid = "GPU-" + str(props.uuid)
+    except Exception:
+        pass
+
+    cfg, model = kelvin_helmholtz(NX, NY, precision="fp64")
+    cells = cfg.interior_cells
+    s = Solver(cfg).init_model(model)
+    s.step(args.warmup)
+    s.sync()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-timed FP64 run ----
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    with ClockSampler(uuid) as clk:
+        e0.record(s.stream)
+        s.step(args.steps)
+        e1.record(s.stream)
+        e1.synchronize()
+    info = s.sync()
+    if info.status != 0 or info.steps != args.warmup + args.steps:
+        raise RuntimeError(f"solver failed: status {info.status} steps {info.steps}")
+    t_fp64 = e0.elapsed_time(e1) / 1e3
+    barrier()
+    if ws > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([t_fp64], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_fp64 = float(tt.item())
+    value = ws * cells * args.steps / t_fp64
+    U64 = s.get_state_numpy()
+
+    # ---- FP32-mixed on the same workload (same warm-up + steps) ----
+    cfgm, _ = kelvin_helmholtz(NX, NY, precision="mixed")
+    m = Solver(cfgm).init_model(model)
+    m.step(args.warmup)
+    m.sync()
+    barrier()
+    e0.record(m.stream)
+    m.step(args.steps)
+    e1.record(m.stream)
+    e1.synchronize()
+    im = m.sync()
+    t_mx = e0.elapsed_time(e1) / 1e3
+    Um = m.get_state_numpy()
+    a = Um[:, 1:-1, 1:-1].reshape(9, -1)
+    b = U64[:, 1:-1, 1:-1].reshape(9, -1)
+    den = np.abs(b).sum(axis=1)
+    l1 = np.abs(a - b).sum(axis=1) / np.where(den > 0, den, 1)
+    names = ["mx", "my", "mz", "en", "ro", "bx", "by", "bz", "ps"]
+    del m
+
+    # ---- end to end through the C ABI with host buffers ----
+    lib = _lib.load()
+    h = s._h
+    host = torch.empty(cfg.shape, dtype=torch.float64).pin_memory()
+    host.copy_(torch.from_numpy(U64))
+    nbytes = host.numel() * 8
+    ke2e = max(3, min(args.steps, 20))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(ke2e):
+        st1 = lib.omhd_solver_put_state(h, host.data_ptr(), 0.0)
+        st2 = lib.omhd_solver_step(h, 1)
+        st3 = lib.omhd_solver_get_state(h, host.data_ptr())
+        if st1 or st2 or st3:
+            raise RuntimeError("e2e call failed")
+    t_e2e = time.perf_counter() - t0
+    e2e = {"value": ws * cells * ke2e / t_e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes,
+           "d2h_bytes_per_step": nbytes, "steps": ke2e,
+           "path": "omhd_solver_put_state(host pinned U) + omhd_solver_step(1) + omhd_solver_get_state(host U)"}
+
+    peaks, peak_src = _peaks()
+    flops_cu = _load_flops()
+    fp64_peak = _fp64_peak_gflops(lib)
+    launch_s = t_fp64 / (2 * args.steps)  # two stage launches per step, nothing else in the region
+    ach_tflops = flops_cu * cells / 2 / launch_s / 1e12
+    hbm_gbs = BYTES_PER_CELL_UPDATE_2D * cells / (t_fp64 / args.steps) / 1e9
+    roofline = {
+        "bound": "fp64", "achieved": ach_tflops, "peak": fp64_peak / 1e3, "unit": "TFLOP/s",
+        "frac": ach_tflops / (fp64_peak / 1e3),
+        "traffic": _load_traffic("stage2d_fp64_kh4096x2048.md"),
+        "peak_source": "DFMA throughput measured in this run (omhd_probe_fp64_peak); "
+                       "MEASURED_PEAKS.json has no FP64 entry",
+        "flops_per_cell_update": flops_cu,
+        "kernel": "omhd::v_fp64::k_stage2d<double,HLLD>",
+        "hbm": {"achieved": hbm_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                "frac": hbm_gbs / peaks.get("hbm_gbs", 1.0), "peak_source": peak_src,
+                "bytes_per_cell_update": BYTES_PER_CELL_UPDATE_2D},
+    }
+    line = {
+        "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_fp64 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded KH initial state)",
+        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "precision": "fp64", "cfl": 0.4,
+                   "l2": "state 605 MB > 129 MB L2: no flush needed", "parallelism": f"replicas{ws}"},
+        "roofline": roofline,
+        "gpu_launches": 2 * args.steps,
+        "e2e": e2e,
+        "clocks": clk.summary(),
+        "mixed": {"value": ws * cells * args.steps / t_mx, "speedup_vs_fp64": t_fp64 / t_mx,
+                  "rel_l1_vs_fp64": dict(zip(names, [float(x) for x in l1])), "status": im.status,
+                  "steps_compared": args.warmup + args.steps},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"], _ = cpu_baseline(steps_budget_s=10.0)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def _fp64_peak_gflops(lib) -> float:
+    import ctypes as C
+
+    g = C.c_double()
+    if lib.omhd_probe_fp64_peak(C.byref(g)) != 0:
+        return float("nan")
+    return g.value
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    from openmhd_gb300.build import build
+    from oracle import oracle
+
+    build()
+    oracle.build()
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

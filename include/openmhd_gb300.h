@@ -1,0 +1,270 @@
+/*
+ * openmhd_gb300.h -- C ABI of the GB300-native OpenMHD step (sm_103a).
+ *
+ * Two layers:
+ *
+ *  1. Routine-level entry points with the reference's argument lists and array
+ *     layout.  Arrays are Fortran column-major double arrays U(ix,jx[,kx],var)
+ *     (i fastest, variable slowest, one ghost cell per side), variable slots
+ *     as in param.h:6-15.  Pointers may be host or device memory (detected
+ *     with cudaPointerGetAttributes); host arrays go through a cached device
+ *     mirror and the call returns with the results in host memory, device
+ *     arrays are processed in place on the library's current stream.
+ *       - omhd_<routine>_2d / _3d : C calling convention, scalars by value,
+ *         returns an omhd_status_t.
+ *       - <routine>_ : gfortran link-level drop-ins for the 2D drivers (every
+ *         argument by reference, lowercase name + trailing underscore, void).
+ *         Failures are recorded for omhd_last_error() and, unless
+ *         omhd_set_abort_on_error(0) was called, end the process with the
+ *         reference's message, as the reference's `stop` does.
+ *
+ *  2. A fused solver handle (omhd_solver) that advances a whole grid by full
+ *     TVD-RK2 steps with two fused stage kernels per step, keeps dt/ch on the
+ *     device and never synchronises inside a step.
+ *
+ * Errors never trap the GPU: kernels record the first failure in a device
+ * error word that the host reads.
+ */
+#ifndef OPENMHD_GB300_H
+#define OPENMHD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OMHD_ABI_VERSION 1
+
+typedef enum {
+  OMHD_OK = 0,
+  OMHD_NEG_PRESSURE = 1,   /* u2v.f90:34-38 "negative pressure" */
+  OMHD_NEG_DENSITY = 2,    /* u2v.f90:39-43 "negative density" */
+  OMHD_DT_TOO_SMALL = 3,   /* set_dt.f90:55-65 "dt is too small" */
+  OMHD_BAD_ARG = 4,        /* invalid size, direction or type */
+  OMHD_TIMEOUT = 5,        /* a bounded device wait gave up */
+  OMHD_CUDA_ERR = 6,       /* CUDA runtime failure */
+  OMHD_NOT_SUPPORTED = 7,  /* option combination not built */
+  OMHD_IO_ERR = 8          /* snapshot file error (fileio.f90:77-82) */
+} omhd_status_t;
+
+typedef struct {
+  int code;        /* omhd_status_t */
+  int i, j, k;     /* 1-based Fortran location of the offending cell, 0 if none */
+  int instance;    /* ensemble member (batched runs), else 0 */
+  double value;    /* offending value (pressure, density or dt) */
+  char message[160];
+} omhd_error_info;
+
+/* ---- scheme switches (2D_basic/main.f90:16-21) ---- */
+enum { OMHD_LM_FLAT = 0, OMHD_LM_MINMOD = 1, OMHD_LM_MC = 2, OMHD_LM_VANLEER = 3, OMHD_LM_KOREN = 4 };
+enum { OMHD_FLUX_LLF = 0, OMHD_FLUX_HLL = 1, OMHD_FLUX_HLLC = 2, OMHD_FLUX_HLLD = 3, OMHD_FLUX_LHLLD = 4 };
+enum { OMHD_TIME_TVDRK2 = 0, OMHD_TIME_RK2 = 1 };
+
+/* ---- boundaries ---- side order: west, east, south, north, down, up */
+enum { OMHD_BC_PERIODIC = 0, OMHD_BC_MIRROR = 1 };
+/* flip masks (bit = variable slot) for the reference's wall conditions */
+#define OMHD_FLIP(slot) (1 << ((slot) - 1)) /* slot is the 1-based param.h index */
+
+/* ---- resistivity models ---- */
+enum {
+  OMHD_ETA_NONE = 0,
+  OMHD_ETA_RECON2D = 1,   /* 2D_reconnection/flux_resistive.f90:1-16 */
+  OMHD_ETA_HARRIS_XZ = 2  /* 1e-3 + (1/60) exp(-(x^2+z^2)/4) */
+};
+
+/* ---- arithmetic of the fused step ---- */
+enum {
+  OMHD_PREC_FP64 = 0,        /* FP64 throughout, multiply-add contraction on */
+  OMHD_PREC_FP64_PARITY = 1, /* FP64, no contraction: the reference's IEEE op sequence */
+  OMHD_PREC_MIXED = 2        /* FP32 reconstruction + Riemann solver, FP64 state/update/dt */
+};
+
+/* ======================================================================
+ * Routine-level entry points, C convention (0 = OMHD_OK)
+ * ==================================================================== */
+
+/* u2v: 2D_basic/u2v.f90:1-46 ; 3D_basic/u2v.f90:1-48 */
+int omhd_u2v_2d(const double* U, double* V, int ix, int jx);
+int omhd_u2v_3d(const double* U, double* V, int ix, int jx, int kx);
+
+/* limiter: 2D_basic/limiter.f90:1-318 ; 3D_basic/limiter.f90:1-419 */
+int omhd_limiter_2d(const double* wk, double* wL, double* wR, int ix, int jx, int dir, int type);
+int omhd_limiter_3d(const double* wk, double* wL, double* wR, int ix, int jx, int kx, int dir, int type);
+
+/* flux_solver: 2D_basic/flux_solver.f90:1-795 ; 3D_basic/flux_solver.f90:1-811 */
+int omhd_flux_solver_2d(double* F, const double* VL, const double* VR, double ch, int ix, int jx,
+                        int dir, int type);
+int omhd_flux_solver_3d(double* F, const double* VL, const double* VR, double ch, int ix, int jx,
+                        int kx, int dir, int type);
+
+/* rk_tvd21/22, rk_std21/22: 2D_basic/rk.f90:9-131 ; 3D_basic/rk.f90:9-147 (dx == dy == dz) */
+int omhd_rk_tvd21_2d(const double* U, double* U1, const double* F, const double* G, double dt,
+                     double dx, int ix, int jx);
+int omhd_rk_tvd22_2d(double* U, const double* U1, const double* F, const double* G, double dt,
+                     double dx, int ix, int jx);
+int omhd_rk_std21_2d(const double* U, double* U1, const double* F, const double* G, double dt,
+                     double dx, int ix, int jx);
+int omhd_rk_std22_2d(double* U, const double* F, const double* G, double dt, double dx, int ix, int jx);
+int omhd_rk_tvd21_3d(const double* U, double* U1, const double* F, const double* G, const double* H,
+                     double dt, double dx, int ix, int jx, int kx);
+int omhd_rk_tvd22_3d(double* U, const double* U1, const double* F, const double* G, const double* H,
+                     double dt, double dx, int ix, int jx, int kx);
+int omhd_rk_std21_3d(const double* U, double* U1, const double* F, const double* G, const double* H,
+                     double dt, double dx, int ix, int jx, int kx);
+int omhd_rk_std22_3d(double* U, const double* F, const double* G, const double* H, double dt,
+                     double dx, int ix, int jx, int kx);
+
+/* glm_ss2: 2D_basic/glm_ss2.f90:1-39 (whole array incl. ghosts) ; 3D_basic/glm_ss2.f90 */
+int omhd_glm_ss2_2d(double* U, double ch, double dt, int ix, int jx);
+int omhd_glm_ss2_3d(double* U, double ch, double dt, int ix, int jx, int kx);
+
+/* set_dt: 2D_basic/set_dt.f90:1-68 ; 3D_basic/set_dt.f90:1-74.  vmax (== ch) and dt out. */
+int omhd_set_dt_2d(const double* U, const double* V, double* vmax, double* dt, double dx, double cfl,
+                   int ix, int jx);
+int omhd_set_dt_3d(const double* U, const double* V, double* vmax, double* dt, double dx, double cfl,
+                   int ix, int jx, int kx);
+
+/* set_dt_resistive: 2D_reconnection/flux_resistive.f90:18-25 (host scalar routine) */
+int omhd_set_dt_resistive(double* dt, double dx, double cfl, int eta_kind);
+
+/* bc: 2D_basic/bc.f90:1-16, 3D_basic/bc.f90 (all periodic) and the wall variants
+ * 2D_KH/bc.f90:6-38, 2D_reconnection/bc.f90:6-50, 3D_reconnection_gpu/bc.cuf:7-98,
+ * expressed as a kind and a sign-flip mask per side. */
+int omhd_bc_2d(double* U, int ix, int jx, const int kind[4], const int flip[4]);
+int omhd_bc_3d(double* U, int ix, int jx, int kx, const int kind[6], const int flip[6]);
+
+/* face-state fix at the domain edges: main.f90:101-102,119-120 (periodic);
+ * bc_for_F/G 2D_KH/bc.f90:42-83, 2D_reconnection/bc.f90:136-197;
+ * bc_for_F/G/H 3D_reconnection_gpu/bc.cuf:103-218 */
+int omhd_facefix_2d(double* VL, double* VR, int ix, int jx, int dir, int kind_lo, int flip_lo,
+                    int kind_hi, int flip_hi);
+int omhd_facefix_3d(double* VL, double* VR, int ix, int jx, int kx, int dir, int kind_lo,
+                    int flip_lo, int kind_hi, int flip_hi);
+
+/* flux_resistive: 2D_reconnection/flux_resistive.f90:27-115 ;
+ * 3D_reconnection_gpu/flux_resistive.cuf:11-140 (x, y, z: cell-centre coordinates) */
+int omhd_flux_resistive_2d(double* F, const double* U, const double* x, const double* y, double dx,
+                           int ix, int jx, int dir, int eta_kind);
+int omhd_flux_resistive_3d(double* F, const double* U, const double* x, const double* y,
+                           const double* z, double dx, int ix, int jx, int kx, int dir, int eta_kind);
+
+/* ======================================================================
+ * gfortran link-level drop-ins for the 2D reference drivers
+ * (2D_basic/main.f90 calls these names with these argument lists)
+ * ==================================================================== */
+void u2v_(const double* U, double* V, const int* ix, const int* jx);
+void limiter_(const double* wk, double* wL, double* wR, const int* ix, const int* jx, const int* dir,
+              const int* type);
+void flux_solver_(double* F, const double* VL, const double* VR, const double* ch, const int* ix,
+                  const int* jx, const int* dir, const int* type);
+void rk_tvd21_(const double* U, double* U1, const double* F, const double* G, const double* dt,
+               const double* dx, const int* ix, const int* jx);
+void rk_tvd22_(double* U, const double* U1, const double* F, const double* G, const double* dt,
+               const double* dx, const int* ix, const int* jx);
+void rk_std21_(const double* U, double* U1, const double* F, const double* G, const double* dt,
+               const double* dx, const int* ix, const int* jx);
+void rk_std22_(double* U, const double* F, const double* G, const double* dt, const double* dx,
+               const int* ix, const int* jx);
+void glm_ss2_(double* U, const double* ch, const double* dt, const int* ix, const int* jx);
+void set_dt_(const double* U, const double* V, double* vmax, double* dt, const double* dx,
+             const double* cfl, const int* ix, const int* jx);
+void bc_(double* U, const int* ix, const int* jx);
+void flux_resistive_(double* F, const double* U, const double* x, const double* y, const double* dx,
+                     const int* ix, const int* jx, const int* dir);
+void set_dt_resistive_(double* dt, const double* dx, const double* cfl);
+
+/* ======================================================================
+ * Library control
+ * ==================================================================== */
+int omhd_abi_version(void);
+/* stream used by the routine-level entry points (NULL = legacy default stream) */
+int omhd_set_stream(void* cuda_stream);
+/* reference semantics for the `_` drop-ins: 1 = print and exit(1) on failure (default) */
+void omhd_set_abort_on_error(int on);
+/* last failure of a routine-level call (synchronises the stream) */
+int omhd_last_error(omhd_error_info* info);
+void omhd_clear_error(void);
+/* frees the cached device mirrors used for host-pointer calls */
+void omhd_release_host_mirrors(void);
+/* measured FP64 FMA throughput of the current GPU in GFLOP/s (roofline denominator;
+ * no counterpart in the reference) */
+int omhd_probe_fp64_peak(double* gflops);
+
+/* ======================================================================
+ * Fused solver handle
+ * ==================================================================== */
+typedef struct omhd_solver omhd_solver;
+
+typedef struct {
+  int nd;              /* 2 or 3 */
+  int ix, jx, kx;      /* array extents incl. one ghost per side (kx = 1 in 2D) */
+  double dx, dy, dz;   /* spacings (the reference uses dx = dy = dz) */
+  double x0, y0, z0;   /* lower domain corner: x(1) = x0 - dx/2 (2D_basic/model.f90:19-28) */
+  double cfl;          /* CFL number (main.f90:15) */
+  double gamma;        /* ratio of specific heats (param.h:3) */
+  int lm_type;         /* OMHD_LM_* */
+  int flux_type;       /* OMHD_FLUX_* */
+  int time_type;       /* OMHD_TIME_* */
+  int eta_kind;        /* OMHD_ETA_*: resistive fluxes + set_dt_resistive when != NONE */
+  int bc_kind[6];      /* OMHD_BC_* per side */
+  int bc_flip[6];      /* sign-flip masks per side (mirror sides) */
+  int precision;       /* OMHD_PREC_* */
+  double tend;         /* end time: steps stop at the first t >= tend (main.f90:73); <= 0: none */
+} omhd_config;
+
+typedef struct {
+  double t;            /* simulation time */
+  double dt;           /* last step's dt */
+  double ch;           /* last step's GLM speed (== vmax) */
+  double vmax_next;    /* fastest wave speed of the current state (next step's ch) */
+  long long steps;     /* completed steps */
+  int done;            /* 1 once t >= tend */
+  int status;          /* first failure (omhd_status_t) */
+} omhd_step_info;
+
+/* model initial states (reference-style problem setups) */
+typedef struct {
+  int kind;            /* 0 Orszag-Tang (2D_basic/model.f90), 1 KH shear layer, 2 Harris sheet (3D) */
+  double amp;          /* OT: B amplitude scale (1); KH: shear speed; Harris: A_y amplitude */
+  double bx0;          /* KH: uniform Bx */
+  double phase_x, phase_y;  /* OT phase shifts (0, 0) */
+  double beta;         /* Harris plasma beta */
+  double pert;         /* KH: vy perturbation amplitude */
+  uint64_t seed;       /* seeded deviates (SplitMix64) */
+} omhd_model;
+
+int omhd_solver_create(const omhd_config* cfg, omhd_solver** out);
+int omhd_solver_destroy(omhd_solver* s);
+/* stream for all work of this handle (NULL = the legacy default stream) */
+int omhd_solver_set_stream(omhd_solver* s, void* cuda_stream);
+/* Bind caller-owned device arrays (ix*jx*kx*9 doubles each) for the state U
+ * and the stage buffer U1.  Unbound handles allocate their own. */
+int omhd_solver_bind(omhd_solver* s, double* U_dev, double* U1_dev);
+/* device pointer of the state array */
+int omhd_solver_state_ptr(omhd_solver* s, double** U_dev);
+/* copy a full state (ghosts included) in / out; host or device pointer.
+ * put_state applies the boundary conditions and computes the first dt. */
+int omhd_solver_put_state(omhd_solver* s, const double* U, double t);
+int omhd_solver_get_state(omhd_solver* s, double* U);
+/* fill the state with a model (2D_basic/model.f90 style), apply bc, compute dt */
+int omhd_solver_init_model(omhd_solver* s, const omhd_model* m);
+/* cell-centre coordinates (reference recurrence x(i) = x(i-1) + dx), host arrays */
+int omhd_solver_coords(omhd_solver* s, double* x, double* y, double* z);
+/* end time (main.f90:73): steps stop on the device at the first t >= tend; <= 0: none */
+int omhd_solver_set_tend(omhd_solver* s, double tend);
+/* enqueue n full steps (asynchronous: returns before the GPU finishes) */
+int omhd_solver_step(omhd_solver* s, int nsteps);
+/* capture n steps once into a CUDA graph and replay it `replays` times */
+int omhd_solver_step_graph(omhd_solver* s, int nsteps, int replays);
+/* wait for the GPU and read the step record; returns the first failure */
+int omhd_solver_sync(omhd_solver* s, omhd_step_info* info);
+int omhd_solver_last_error(omhd_solver* s, omhd_error_info* info);
+/* kernels launched by the last omhd_solver_step call per step (for accounting) */
+int omhd_solver_launches_per_step(omhd_solver* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OPENMHD_GB300_H */

@@ -1,0 +1,41 @@
+// omhd_fused.h -- host-visible argument blocks and launchers of the fused
+// stage kernels.  Each arithmetic variant lives in its own translation unit
+// (compiled with its own floating-point flags) and exports one launcher.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace omhd {
+
+struct StepState;
+struct DevError;
+
+struct StageArgs {
+  const double* Uin;    // state the fluxes are built from (stage 1: U, stage 2: U1)
+  const double* Ubase;  // state the update starts from (U; its psi gets the GLM factor)
+  const double* U1;     // stage 2 (TVD): the stage-1 result, else nullptr
+  double* Uout;         // stage 1: U1 ; stage 2: U (in place)
+  int ix, jx, kx;       // extents incl. ghosts (kx = 1 in 2D)
+  int nd;
+  double dx, dy, dz;
+  double dtx_scale;     // 1.0, or 0.5 for the first stage of standard RK2 (rk.f90:76)
+  double gamma;
+  int lm_type, flux_type, time_type, stage, iso;
+  int bc_kind[6], bc_flip[6];
+  int eta_kind;
+  const double* xc;     // cell-centre coordinates (resistive runs)
+  const double* yc;
+  const double* zc;
+  StepState* st;
+  DevError* err;
+  double cfl, dmin;     // for the end-of-step dt planning
+};
+
+// launchers: return 0 or a CUDA error code
+int launch_stage2d_fp64(const StageArgs& a, cudaStream_t s);
+int launch_stage2d_parity(const StageArgs& a, cudaStream_t s);
+int launch_stage2d_mixed(const StageArgs& a, cudaStream_t s);
+int launch_stage3d_fp64(const StageArgs& a, cudaStream_t s);
+int launch_stage3d_parity(const StageArgs& a, cudaStream_t s);
+int launch_stage3d_mixed(const StageArgs& a, cudaStream_t s);
+
+}  // namespace omhd

@@ -1,0 +1,341 @@
+// omhd_riemann.cuh -- face reconstruction (slope limiters) and numerical
+// fluxes, as device templates over the arithmetic type T (double or float)
+// and the face direction DIR (1,2,3).
+//
+// Face states use the reference's VL/VR slot order (main.f90:91-99):
+//   w = (vx, vy, vz, p, rho, Bx, By, Bz, psi)
+// and fluxes the conserved slot order (mx, my, mz, E, rho, Bx, By, Bz, psi).
+// Every formula keeps the reference's operation order so that a translation
+// unit built with --fmad=false reproduces the reference arithmetic exactly;
+// the performance build of the same source lets the compiler contract
+// multiply-adds.
+#pragma once
+#include "omhd_common.cuh"
+
+namespace omhd {
+
+enum { LM_FLAT = 0, LM_MINMOD = 1, LM_MC = 2, LM_VANLEER = 3, LM_KOREN = 4 };
+enum { FX_LLF = 0, FX_HLL = 1, FX_HLLC = 2, FX_HLLD = 3, FX_LHLLD = 4 };
+
+// Slope-limited reconstruction of one cell (2D_basic/limiter.f90):
+//   right = state at the cell's lower face   (wR(i-1) in the reference)
+//   left  = state at the cell's upper face   (wL(i)   in the reference)
+// minmod :98, MC :141-158, van Leer :201-210, Koren :256-272, flat :54-71.
+template <class T>
+__device__ __forceinline__ void reconstruct(int type, T wm, T w0, T wp, T& left, T& right) {
+  const T gA = (w0 - wm);
+  const T gB = (wp - w0);
+  T grad;
+  switch (type) {
+    case LM_MINMOD:
+      grad = (fsign(T(0.25), gA) + fsign(T(0.25), gB)) * fmin2(fabs(gA), fabs(gB));
+      right = w0 - grad;
+      left = w0 + grad;
+      break;
+    case LM_MC: {
+      const T gC = T(0.25) * (wp - wm);
+      grad = (fsign(T(0.5), gA) + fsign(T(0.5), gB)) * fmin2(fmin2(fabs(gA), fabs(gB)), fabs(gC));
+      right = w0 - grad;
+      left = w0 + grad;
+      break;
+    }
+    case LM_VANLEER:
+      if (gA * gB <= T(0))
+        grad = T(0);
+      else
+        grad = gA * gB / (gA + gB);
+      right = w0 - grad;
+      left = w0 + grad;
+      break;
+    case LM_KOREN: {
+      const T f6 = T(1) / T(6);
+      T gC = f6 * (2 * gA + gB);
+      right = w0 - (fsign(T(0.5), gA) + fsign(T(0.5), gB)) * fmin2(fmin2(fabs(gA), fabs(gB)), fabs(gC));
+      gC = f6 * (gA + 2 * gB);
+      left = w0 + (fsign(T(0.5), gA) + fsign(T(0.5), gB)) * fmin2(fmin2(fabs(gA), fabs(gB)), fabs(gC));
+      break;
+    }
+    default:  // flat: the state itself on both faces
+      right = w0;
+      left = w0;
+  }
+}
+
+// Numerical flux across one face (2D_basic/flux_solver.f90):
+//   LLF :89-148, HLL :153-221, HLLC :226-347, HLLD :352-585 (HLLC-G fallback
+//   :447-476), LHLLD :590-789; GLM fluxes for Bn and psi :580-581.
+// r1 = 1/(gamma-1), r2 = gamma/(gamma-1) are passed in (flux_solver.f90:38-39).
+template <class T, int DIR, int TYPE>
+__device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV], T ch, T gamma, T r1,
+                                             T r2, T (&Fo)[NV]) {
+  constexpr int vn = VX + (DIR - 1) % 3, vt1 = VX + DIR % 3, vt2 = VX + (DIR + 1) % 3;
+  constexpr int bn = BX + (DIR - 1) % 3, bt1 = BX + DIR % 3, bt2 = BX + (DIR + 1) % 3;
+  constexpr int mn = MX + (DIR - 1) % 3, mt1 = MX + DIR % 3, mt2 = MX + (DIR + 1) % 3;
+  const T hllg_factor = T(1.001);
+  const T ch2 = ch * ch;
+
+  T UL[4], UR[4], FL[NV], FR[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    FL[v] = T(0);
+    FR[v] = T(0);
+    Fo[v] = T(0);
+  }
+  T v2, B2, vBL, vBR, f1, f2, aL, aR, ptL = T(0), ptR = T(0), aL1 = T(0), aR1 = T(0);
+
+  // VL --> UL, FL  (:359-372)
+  v2 = L[VX] * L[VX] + L[VY] * L[VY] + L[VZ] * L[VZ];
+  B2 = L[BX] * L[BX] + L[BY] * L[BY] + L[BZ] * L[BZ];
+  vBL = L[VX] * L[BX] + L[VY] * L[BY] + L[VZ] * L[BZ];
+  UL[MX] = L[RO] * L[VX];
+  UL[MY] = L[RO] * L[VY];
+  UL[MZ] = L[RO] * L[VZ];
+  UL[EN] = T(0.5) * (L[RO] * v2 + B2) + r1 * L[PR];
+  FL[RO] = L[RO] * L[vn];
+  FL[mn] = L[RO] * L[vn] * L[vn] - L[bn] * L[bn] + L[PR] + T(0.5) * B2;
+  FL[mt1] = L[RO] * L[vn] * L[vt1] - L[bn] * L[bt1];
+  FL[mt2] = L[RO] * L[vn] * L[vt2] - L[bn] * L[bt2];
+  FL[EN] = (T(0.5) * L[RO] * v2 + r2 * L[PR] + B2) * L[vn] - vBL * L[bn];
+  FL[bt1] = L[vn] * L[bt1] - L[bn] * L[vt1];
+  FL[bt2] = L[vn] * L[bt2] - L[bn] * L[vt2];
+  f1 = gamma * L[PR];
+  f2 = 4 * (L[bn] * L[bn]);
+  if (TYPE == FX_LLF) {
+    aL = sqrt(((f1 + B2) + sqrt((f1 + B2) * (f1 + B2) - f1 * f2)) / (2 * L[RO]));
+  } else {
+    aL = ((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f1 * f2, T(0)))) / (2 * L[RO]);
+    ptL = L[PR] + T(0.5) * B2;
+    if (TYPE == FX_LHLLD) {
+      const T g1 = L[RO] * v2;
+      aL1 = ((g1 + B2) + sqrt(fmax2((g1 + B2) * (g1 + B2) - g1 * f2, T(0)))) / (2 * L[RO]);
+    }
+  }
+
+  // VR --> UR, FR  (:381-401)
+  v2 = R[VX] * R[VX] + R[VY] * R[VY] + R[VZ] * R[VZ];
+  B2 = R[BX] * R[BX] + R[BY] * R[BY] + R[BZ] * R[BZ];
+  vBR = R[VX] * R[BX] + R[VY] * R[BY] + R[VZ] * R[BZ];
+  UR[MX] = R[RO] * R[VX];
+  UR[MY] = R[RO] * R[VY];
+  UR[MZ] = R[RO] * R[VZ];
+  UR[EN] = T(0.5) * (R[RO] * v2 + B2) + r1 * R[PR];
+  FR[RO] = R[RO] * R[vn];
+  FR[mn] = R[RO] * R[vn] * R[vn] - R[bn] * R[bn] + R[PR] + T(0.5) * B2;
+  FR[mt1] = R[RO] * R[vn] * R[vt1] - R[bn] * R[bt1];
+  FR[mt2] = R[RO] * R[vn] * R[vt2] - R[bn] * R[bt2];
+  FR[EN] = (T(0.5) * R[RO] * v2 + r2 * R[PR] + B2) * R[vn] - vBR * R[bn];
+  FR[bt1] = R[vn] * R[bt1] - R[bn] * R[vt1];
+  FR[bt2] = R[vn] * R[bt2] - R[bn] * R[vt2];
+  f1 = gamma * R[PR];
+  f2 = 4 * (R[bn] * R[bn]);
+  if (TYPE == FX_LLF) {
+    aR = sqrt(((f1 + B2) + sqrt((f1 + B2) * (f1 + B2) - f1 * f2)) / (2 * R[RO]));
+  } else {
+    aR = ((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f1 * f2, T(0)))) / (2 * R[RO]);
+    ptR = R[PR] + T(0.5) * B2;
+    if (TYPE == FX_LHLLD) {
+      const T g1 = R[RO] * v2;
+      aR1 = ((g1 + B2) + sqrt(fmax2((g1 + B2) * (g1 + B2) - g1 * f2, T(0)))) / (2 * R[RO]);
+    }
+  }
+
+  if (TYPE == FX_LLF) {  // :138-142
+    f1 = fmax2(fabs(L[vn]) + aL, fabs(R[vn]) + aR);
+#pragma unroll
+    for (int v = MX; v <= EN; ++v) Fo[v] = T(0.5) * (FL[v] + FR[v] - f1 * (UR[v] - UL[v]));
+    Fo[RO] = T(0.5) * (FL[RO] + FR[RO] - f1 * (R[RO] - L[RO]));
+    Fo[bt1] = T(0.5) * (FL[bt1] + FR[bt1] - f1 * (R[bt1] - L[bt1]));
+    Fo[bt2] = T(0.5) * (FL[bt2] + FR[bt2] - f1 * (R[bt2] - L[bt2]));
+  } else if (TYPE == FX_HLL) {  // :205-214
+    f1 = sqrt(fmax2(aL, aR));
+    aL = fmin2(fmin2(L[vn], R[vn]) - f1, T(0));
+    aR = fmax2(fmax2(L[vn], R[vn]) + f1, T(0));
+    f1 = T(1) / (aR - aL);
+    f2 = aL * aR;
+#pragma unroll
+    for (int v = MX; v <= EN; ++v) Fo[v] = f1 * (aR * FL[v] - aL * FR[v] + f2 * (UR[v] - UL[v]));
+    Fo[RO] = f1 * (aR * FL[RO] - aL * FR[RO] + f2 * (R[RO] - L[RO]));
+    Fo[bt1] = f1 * (aR * FL[bt1] - aL * FR[bt1] + f2 * (R[bt1] - L[bt1]));
+    Fo[bt2] = f1 * (aR * FL[bt2] - aL * FR[bt2] + f2 * (R[bt2] - L[bt2]));
+  } else if (TYPE == FX_HLLC) {  // :281-340
+    T Uh[NV];
+    f1 = sqrt(fmax2(aL, aR));
+    aL = fmin2(fmin2(L[vn], R[vn]) - f1, T(0));
+    aR = fmax2(fmax2(L[vn], R[vn]) + f1, T(0));
+    f1 = T(1) / (aR - aL);
+    f2 = aL * aR;
+#pragma unroll
+    for (int v = MX; v <= MZ; ++v) Uh[v] = f1 * (aR * UR[v] - aL * UL[v] - FR[v] + FL[v]);
+#pragma unroll
+    for (int v = RO; v <= BZ; ++v) Uh[v] = f1 * (aR * R[v] - aL * L[v] - FR[v] + FL[v]);
+    Fo[bt1] = f1 * (aR * FL[bt1] - aL * FR[bt1] + f2 * (R[bt1] - L[bt1]));
+    Fo[bt2] = f1 * (aR * FL[bt2] - aL * FR[bt2] + f2 * (R[bt2] - L[bt2]));
+    f2 = T(1) / Uh[RO];
+    const T aM = Uh[mn] * f2;
+    const T at1 = Uh[mt1] * f2;
+    const T at2 = Uh[mt2] * f2;
+    const T pt = ptL + L[RO] * (aL - L[vn]) * (aM - L[vn]);
+    const T roL = L[RO] * (aL - L[vn]) / (aL - aM);
+    const T enL = ((aL - L[vn]) * UL[EN] - ptL * L[vn] + pt * aM +
+                   Uh[bn] * (vBL - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])) /
+                  (aL - aM);
+    const T roR = R[RO] * (aR - R[vn]) / (aR - aM);
+    const T enR = ((aR - R[vn]) * UR[EN] - ptR * R[vn] + pt * aM +
+                   Uh[bn] * (vBR - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])) /
+                  (aR - aM);
+    f1 = T(0.5) + fsign(T(0.5), aM);
+    f2 = T(1) - f1;
+    Fo[mn] = f1 * (aL * (roL * aM - UL[mn]) + FL[mn]) + f2 * (aR * (roR * aM - UR[mn]) + FR[mn]);
+    Fo[mt1] = f1 * (aL * (roL * at1 - UL[mt1]) + FL[mt1]) + f2 * (aR * (roR * at1 - UR[mt1]) + FR[mt1]);
+    Fo[mt2] = f1 * (aL * (roL * at2 - UL[mt2]) + FL[mt2]) + f2 * (aR * (roR * at2 - UR[mt2]) + FR[mt2]);
+    Fo[EN] = f1 * (aL * (enL - UL[EN]) + FL[EN]) + f2 * (aR * (enR - UR[EN]) + FR[EN]);
+    Fo[RO] = f1 * (aL * (roL - L[RO]) + FL[RO]) + f2 * (aR * (roR - R[RO]) + FR[RO]);
+  } else {  // HLLD :408-576 / LHLLD :648-780
+    T psi = T(0);
+    if (TYPE == FX_LHLLD) {
+      f1 = fmin2(T(1), fmax2(aL1, aR1) / fmax2(aL, aR));
+      psi = 2 * sqrt(f1) - f1;
+    }
+    f1 = sqrt(fmax2(aL, aR));
+    aL = fmin2(L[vn], R[vn]) - f1;
+    aR = fmax2(L[vn], R[vn]) + f1;
+    if (aL >= T(0)) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) Fo[v] = FL[v];
+    } else if (aR <= T(0)) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) Fo[v] = FR[v];
+    } else {
+      T Uh[NV];
+      f1 = T(1) / (aR - aL);
+#pragma unroll
+      for (int v = MX; v <= MZ; ++v) Uh[v] = f1 * (aR * UR[v] - aL * UL[v] - FR[v] + FL[v]);
+#pragma unroll
+      for (int v = RO; v <= BZ; ++v) Uh[v] = f1 * (aR * R[v] - aL * L[v] - FR[v] + FL[v]);
+      const T aM = Uh[mn] / Uh[RO];
+      T pt;
+      if (TYPE == FX_LHLLD) {
+        pt = (R[RO] * ptL * (aR - R[vn]) - L[RO] * ptR * (aL - L[vn]) +
+              psi * L[RO] * R[RO] * (aR - R[vn]) * (aL - L[vn]) * (R[vn] - L[vn])) /
+             (R[RO] * (aR - R[vn]) - L[RO] * (aL - L[vn]));
+      } else {
+        pt = ptL + L[RO] * (aL - L[vn]) * (aM - L[vn]);
+      }
+      const T roL = L[RO] * (aL - L[vn]) / (aL - aM);
+      const T roR = R[RO] * (aR - R[vn]) / (aR - aM);
+      const T aVL = fabs(Uh[bn]) / sqrt(roL);
+      const T aVR = fabs(Uh[bn]) / sqrt(roR);
+      if (TYPE == FX_HLLD && ((aL >= (aM - hllg_factor * aVL)) || ((aM + hllg_factor * aVR) >= aR))) {
+        // HLLC-G fallback :450-476
+        f2 = aL * aR;
+        Fo[bt1] = f1 * (aR * FL[bt1] - aL * FR[bt1] + f2 * (R[bt1] - L[bt1]));
+        Fo[bt2] = f1 * (aR * FL[bt2] - aL * FR[bt2] + f2 * (R[bt2] - L[bt2]));
+        const T at1 = Uh[mt1] / Uh[RO];
+        const T at2 = Uh[mt2] / Uh[RO];
+        const T enL = ((aL - L[vn]) * UL[EN] - ptL * L[vn] + pt * aM +
+                       Uh[bn] * (vBL - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])) /
+                      (aL - aM);
+        const T enR = ((aR - R[vn]) * UR[EN] - ptR * R[vn] + pt * aM +
+                       Uh[bn] * (vBR - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])) /
+                      (aR - aM);
+        f1 = T(0.5) + fsign(T(0.5), aM);
+        f2 = T(1) - f1;
+        Fo[mn] = f1 * (aL * (roL * aM - UL[mn]) + FL[mn]) + f2 * (aR * (roR * aM - UR[mn]) + FR[mn]);
+        Fo[mt1] = f1 * (aL * (roL * at1 - UL[mt1]) + FL[mt1]) + f2 * (aR * (roR * at1 - UR[mt1]) + FR[mt1]);
+        Fo[mt2] = f1 * (aL * (roL * at2 - UL[mt2]) + FL[mt2]) + f2 * (aR * (roR * at2 - UR[mt2]) + FR[mt2]);
+        Fo[EN] = f1 * (aL * (enL - UL[EN]) + FL[EN]) + f2 * (aR * (enR - UR[EN]) + FR[EN]);
+        Fo[RO] = f1 * (aL * (roL - L[RO]) + FL[RO]) + f2 * (aR * (roR - R[RO]) + FR[RO]);
+      } else {
+        T UL1[NV], UR1[NV];
+        // L* (:482-493)
+        const T tL = aL - L[vn];
+        f1 = T(1) / (L[RO] * tL * (aL - aM) - Uh[bn] * Uh[bn]);
+        UL1[bt1] = L[bt1] * f1 * (L[RO] * (tL * tL) - Uh[bn] * Uh[bn]);
+        UL1[bt2] = L[bt2] * f1 * (L[RO] * (tL * tL) - Uh[bn] * Uh[bn]);
+        const T vt1L = L[vt1] - f1 * Uh[bn] * L[bt1] * (aM - L[vn]);
+        const T vt2L = L[vt2] - f1 * Uh[bn] * L[bt2] * (aM - L[vn]);
+        UL1[RO] = roL;
+        UL1[EN] = ((aL - L[vn]) * UL[EN] - ptL * L[vn] + pt * aM +
+                   Uh[bn] * (vBL - aM * Uh[bn] - vt1L * UL1[bt1] - vt2L * UL1[bt2])) /
+                  (aL - aM);
+        UL1[mn] = roL * aM;
+        UL1[mt1] = roL * vt1L;
+        UL1[mt2] = roL * vt2L;
+        // R* (:496-507)
+        const T tR = aR - R[vn];
+        f1 = T(1) / (R[RO] * tR * (aR - aM) - Uh[bn] * Uh[bn]);
+        UR1[bt1] = R[bt1] * f1 * (R[RO] * (tR * tR) - Uh[bn] * Uh[bn]);
+        UR1[bt2] = R[bt2] * f1 * (R[RO] * (tR * tR) - Uh[bn] * Uh[bn]);
+        const T vt1R = R[vt1] - f1 * Uh[bn] * R[bt1] * (aM - R[vn]);
+        const T vt2R = R[vt2] - f1 * Uh[bn] * R[bt2] * (aM - R[vn]);
+        UR1[RO] = roR;
+        UR1[EN] = ((aR - R[vn]) * UR[EN] - ptR * R[vn] + pt * aM +
+                   Uh[bn] * (vBR - aM * Uh[bn] - vt1R * UR1[bt1] - vt2R * UR1[bt2])) /
+                  (aR - aM);
+        UR1[mn] = roR * aM;
+        UR1[mt1] = roR * vt1R;
+        UR1[mt2] = roR * vt2R;
+        aL1 = aM - aVL;
+        aR1 = aM + aVR;
+        if (aL1 >= T(0)) {  // F(L*) :514-519
+#pragma unroll
+          for (int v = MX; v <= EN; ++v) Fo[v] = aL * (UL1[v] - UL[v]) + FL[v];
+          Fo[RO] = aL * (UL1[RO] - L[RO]) + FL[RO];
+          Fo[bt1] = aL * (UL1[bt1] - L[bt1]) + FL[bt1];
+          Fo[bt2] = aL * (UL1[bt2] - L[bt2]) + FL[bt2];
+        } else if (aR1 <= T(0)) {  // F(R*) :522-527
+#pragma unroll
+          for (int v = MX; v <= EN; ++v) Fo[v] = aR * (UR1[v] - UR[v]) + FR[v];
+          Fo[RO] = aR * (UR1[RO] - R[RO]) + FR[RO];
+          Fo[bt1] = aR * (UR1[bt1] - R[bt1]) + FR[bt1];
+          Fo[bt2] = aR * (UR1[bt2] - R[bt2]) + FR[bt2];
+        } else {  // central states :533-572
+          T U2[NV];
+          const T roLs = sqrt(roL);
+          const T roRs = sqrt(roR);
+          f1 = T(1) / (roLs + roRs);
+          f2 = fsign(T(1), Uh[bn]);
+          const T at1 = f1 * (roLs * vt1L + roRs * vt1R + (UR1[bt1] - UL1[bt1]) * f2);
+          const T at2 = f1 * (roLs * vt2L + roRs * vt2R + (UR1[bt2] - UL1[bt2]) * f2);
+          U2[bt1] = f1 * (roLs * UR1[bt1] + roRs * UL1[bt1] + roLs * roRs * (vt1R - vt1L) * f2);
+          U2[bt2] = f1 * (roLs * UR1[bt2] + roRs * UL1[bt2] + roLs * roRs * (vt2R - vt2L) * f2);
+          if (aM >= T(0)) {  // F(L**)
+            U2[RO] = roL;
+            U2[EN] = UL1[EN] - roLs * (vt1L * UL1[bt1] + vt2L * UL1[bt2] - at1 * U2[bt1] - at2 * U2[bt2]) * f2;
+            U2[mn] = roL * aM;
+            U2[mt1] = roL * at1;
+            U2[mt2] = roL * at2;
+#pragma unroll
+            for (int v = MX; v <= EN; ++v) Fo[v] = aL1 * U2[v] - (aL1 - aL) * UL1[v] - aL * UL[v] + FL[v];
+            Fo[RO] = aL1 * U2[RO] - (aL1 - aL) * UL1[RO] - aL * L[RO] + FL[RO];
+            Fo[bt1] = aL1 * U2[bt1] - (aL1 - aL) * UL1[bt1] - aL * L[bt1] + FL[bt1];
+            Fo[bt2] = aL1 * U2[bt2] - (aL1 - aL) * UL1[bt2] - aL * L[bt2] + FL[bt2];
+          } else {  // F(R**)
+            U2[RO] = roR;
+            U2[EN] = UR1[EN] + roRs * (vt1R * UR1[bt1] + vt2R * UR1[bt2] - at1 * U2[bt1] - at2 * U2[bt2]) * f2;
+            U2[mn] = roR * aM;
+            U2[mt1] = roR * at1;
+            U2[mt2] = roR * at2;
+#pragma unroll
+            for (int v = MX; v <= EN; ++v) Fo[v] = aR1 * U2[v] - (aR1 - aR) * UR1[v] - aR * UR[v] + FR[v];
+            Fo[RO] = aR1 * U2[RO] - (aR1 - aR) * UR1[RO] - aR * R[RO] + FR[RO];
+            Fo[bt1] = aR1 * U2[bt1] - (aR1 - aR) * UR1[bt1] - aR * R[bt1] + FR[bt1];
+            Fo[bt2] = aR1 * U2[bt2] - (aR1 - aR) * UR1[bt2] - aR * R[bt2] + FR[bt2];
+          }
+        }
+      }
+    }
+  }
+  // GLM fluxes :580-581
+  Fo[bn] = T(0.5) * ((L[PS] + R[PS]) - ch * (R[bn] - L[bn]));
+  Fo[PS] = T(0.5) * (ch2 * (L[bn] + R[bn]) - ch * (R[PS] - L[PS]));
+}
+
+// Fast magnetosonic speed used by set_dt (2D_basic/set_dt.f90:27-34).
+template <class T>
+__device__ __forceinline__ T fast_speed(T f1, T B2, T bd, T ro) {
+  const T f2 = 4 * f1 * (bd * bd);
+  return sqrt(((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f2, T(0)))) / (2 * ro));
+}
+
+}  // namespace omhd

@@ -1,0 +1,208 @@
+// omhd_runtime.cu -- library stream, error record and host-pointer mirrors for
+// the routine-level entry points of libopenmhd_gb300.so.
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "omhd_common.cuh"
+#include "omhd_runtime.h"
+
+namespace omhd {
+
+namespace {
+cudaStream_t g_stream = nullptr;
+DevError* g_dev_error = nullptr;
+unsigned long long* g_dev_accum = nullptr;
+bool g_abort = true;
+omhd_error_info g_last = {};
+
+struct PoolSlot {
+  double* dev = nullptr;
+  size_t cap = 0;
+};
+PoolSlot g_pool[8];
+}  // namespace
+
+cudaStream_t lib_stream() { return g_stream; }
+
+int cuda_status(cudaError_t e, const char* where) {
+  if (e == cudaSuccess) return OMHD_OK;
+  char msg[160];
+  snprintf(msg, sizeof msg, "CUDA error in %s: %s", where, cudaGetErrorString(e));
+  set_host_error(OMHD_CUDA_ERR, 0, 0, 0, 0.0, msg);
+  return OMHD_CUDA_ERR;
+}
+
+DevError* lib_dev_error() {
+  if (!g_dev_error) {
+    if (cudaMalloc(&g_dev_error, sizeof(DevError)) != cudaSuccess) return nullptr;
+    cudaMemsetAsync(g_dev_error, 0, sizeof(DevError), g_stream);
+  }
+  return g_dev_error;
+}
+
+unsigned long long* lib_dev_accum() {
+  if (!g_dev_accum) {
+    if (cudaMalloc(&g_dev_accum, sizeof(unsigned long long)) != cudaSuccess) return nullptr;
+  }
+  return g_dev_accum;
+}
+
+void set_host_error(int code, int i, int j, int k, double value, const char* msg) {
+  if (g_last.code != OMHD_OK) return;  // keep the first failure
+  g_last.code = code;
+  g_last.i = i;
+  g_last.j = j;
+  g_last.k = k;
+  g_last.instance = 0;
+  g_last.value = value;
+  snprintf(g_last.message, sizeof g_last.message, "%s", msg ? msg : "");
+}
+
+bool abort_on_error() { return g_abort; }
+
+int finish_status(int code) {
+  if (code != OMHD_OK && g_abort) {
+    fprintf(stdout, " %s\n", g_last.message);
+    fflush(stdout);
+    exit(1);
+  }
+  return code;
+}
+
+ArgSet::~ArgSet() {}
+
+double* ArgSet::add(const double* p, size_t count, bool copy_in, bool copy_out) {
+  if (status_) return nullptr;
+  if (!p) {
+    status_ = OMHD_BAD_ARG;
+    return nullptr;
+  }
+  cudaPointerAttributes attr;
+  cudaError_t e = cudaPointerGetAttributes(&attr, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    attr.type = cudaMemoryTypeUnregistered;
+  }
+  if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) {
+    return const_cast<double*>(p);
+  }
+  if (n_ >= 8) {
+    status_ = OMHD_BAD_ARG;
+    return nullptr;
+  }
+  PoolSlot& ps = g_pool[n_];
+  if (ps.cap < count) {
+    if (ps.dev) cudaFree(ps.dev);
+    ps.dev = nullptr;
+    ps.cap = 0;
+    if (cuda_status(cudaMalloc(&ps.dev, count * sizeof(double)), "host mirror allocation")) {
+      status_ = OMHD_CUDA_ERR;
+      return nullptr;
+    }
+    ps.cap = count;
+  }
+  if (copy_in) {
+    if (cuda_status(cudaMemcpyAsync(ps.dev, p, count * sizeof(double), cudaMemcpyHostToDevice, g_stream),
+                    "host mirror copy-in")) {
+      status_ = OMHD_CUDA_ERR;
+      return nullptr;
+    }
+  }
+  slots_[n_] = Slot{const_cast<double*>(p), ps.dev, count, copy_out};
+  ++n_;
+  any_host_ = true;
+  return ps.dev;
+}
+
+int ArgSet::finish() {
+  if (status_) return status_;
+  for (int s = 0; s < n_; ++s) {
+    if (!slots_[s].out) continue;
+    if (cuda_status(cudaMemcpyAsync(slots_[s].host, slots_[s].dev, slots_[s].count * sizeof(double),
+                                    cudaMemcpyDeviceToHost, g_stream),
+                    "host mirror copy-out"))
+      return OMHD_CUDA_ERR;
+  }
+  if (any_host_) {
+    if (cuda_status(cudaStreamSynchronize(g_stream), "stream synchronize")) return OMHD_CUDA_ERR;
+  }
+  return cuda_status(cudaGetLastError(), "kernel launch");
+}
+
+// FP64 fused multiply-add throughput probe: 8 independent DFMA chains per
+// thread, 2 flops per DFMA.  Used as the FP64 roofline denominator.
+__global__ void k_dfma_probe(double* out, double b, double c, int iters, int flag) {
+  double a0 = 1.0 + threadIdx.x * 1e-7, a1 = a0 + 1e-3, a2 = a0 + 2e-3, a3 = a0 + 3e-3;
+  double a4 = a0 + 4e-3, a5 = a0 + 5e-3, a6 = a0 + 6e-3, a7 = a0 + 7e-3;
+  for (int it = 0; it < iters; ++it) {
+    a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+    a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+  }
+  if (flag) out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+}  // namespace omhd
+
+using namespace omhd;
+
+extern "C" {
+
+int omhd_probe_fp64_peak(double* gflops) {
+  if (!gflops) return OMHD_BAD_ARG;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return OMHD_CUDA_ERR;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  double* out = nullptr;
+  if (cuda_status(cudaMalloc(&out, sizeof(double) * blocks * threads), "probe allocation")) return OMHD_CUDA_ERR;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_dfma_probe<<<blocks, threads>>>(out, 1.0000001, 0.999999, iters, 0);
+  cudaEventRecord(e0);
+  for (int r = 0; r < 5; ++r) k_dfma_probe<<<blocks, threads>>>(out, 1.0000001, 0.999999, iters, 0);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  const double flops = 5.0 * blocks * threads * (double)iters * 8 * 2;
+  *gflops = flops / (ms * 1e6);
+  return cuda_status(cudaGetLastError(), "probe kernel");
+}
+
+int omhd_abi_version(void) { return OMHD_ABI_VERSION; }
+
+int omhd_set_stream(void* s) {
+  g_stream = (cudaStream_t)s;
+  return OMHD_OK;
+}
+
+void omhd_set_abort_on_error(int on) { g_abort = on != 0; }
+
+int omhd_last_error(omhd_error_info* info) {
+  if (g_stream || g_dev_error) cudaStreamSynchronize(g_stream);
+  if (info) *info = g_last;
+  return g_last.code;
+}
+
+void omhd_clear_error(void) {
+  memset(&g_last, 0, sizeof g_last);
+  if (g_dev_error) {
+    cudaMemsetAsync(g_dev_error, 0, sizeof(DevError), g_stream);
+    cudaStreamSynchronize(g_stream);
+  }
+}
+
+void omhd_release_host_mirrors(void) {
+  for (auto& ps : g_pool) {
+    if (ps.dev) cudaFree(ps.dev);
+    ps.dev = nullptr;
+    ps.cap = 0;
+  }
+}
+
+}  // extern "C"

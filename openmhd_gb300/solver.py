@@ -1,0 +1,277 @@
+"""Host-side mirror of the reference's driver loop (2D_basic/main.f90:56-188)
+over the fused GB300 step, plus the problem setups used by this project.
+
+A `Solver` owns one omhd_solver handle.  Its state and stage buffers are
+torch float64 CUDA tensors bound to the handle, shaped (9, jx, ix) in 2D and
+(9, kx, jx, ix) in 3D: exactly the reference's column-major U(ix,jx[,kx],var)
+in memory.  Work runs on the solver's own CUDA stream, and nothing in a step
+synchronises with the host.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+from . import _lib
+
+LIMITERS = {"flat": 0, "minmod": 1, "mc": 2, "vanleer": 3, "koren": 4}
+FLUXES = {"llf": 0, "hll": 1, "hllc": 2, "hlld": 3, "lhlld": 4}
+PRECISIONS = {"fp64": 0, "fp64_parity": 1, "mixed": 2}
+ETA = {"none": 0, "recon2d": 1, "harris_xz": 2}
+
+# variable slots (param.h:6-15), 1-based as in the reference
+MX, MY, MZ, EN, RO, BX, BY, BZ, PS = range(1, 10)
+VAR_NAMES = ["mx", "my", "mz", "en", "ro", "bx", "by", "bz", "ps"]
+
+
+def flip(*slots: int) -> int:
+    """Sign-flip mask for mirror boundaries (bit = 1-based variable slot - 1)."""
+    m = 0
+    for s in slots:
+        m |= 1 << (s - 1)
+    return m
+
+
+class OmhdError(RuntimeError):
+    def __init__(self, code: int, message: str = ""):
+        super().__init__(f"openmhd_gb300 status {code}: {message}")
+        self.code = code
+
+
+@dataclass
+class SolverConfig:
+    nd: int
+    ix: int
+    jx: int
+    kx: int = 1
+    dx: float = 1.0
+    dy: float = 1.0
+    dz: float = 1.0
+    x0: float = 0.0
+    y0: float = 0.0
+    z0: float = 0.0
+    cfl: float = 0.4
+    gamma: float = 5.0 / 3.0
+    limiter: str = "minmod"
+    flux: str = "hlld"
+    time: str = "tvdrk2"
+    eta: str = "none"
+    bc_kind: tuple = (0, 0, 0, 0, 0, 0)
+    bc_flip: tuple = (0, 0, 0, 0, 0, 0)
+    precision: str = "fp64"
+    tend: float = 0.0
+
+    def to_c(self) -> _lib.Config:
+        c = _lib.Config()
+        c.nd, c.ix, c.jx, c.kx = self.nd, self.ix, self.jx, self.kx
+        c.dx, c.dy, c.dz = self.dx, self.dy, self.dz
+        c.x0, c.y0, c.z0 = self.x0, self.y0, self.z0
+        c.cfl, c.gamma = self.cfl, self.gamma
+        c.lm_type = LIMITERS[self.limiter]
+        c.flux_type = FLUXES[self.flux]
+        c.time_type = 0 if self.time == "tvdrk2" else 1
+        c.eta_kind = ETA[self.eta]
+        for q in range(6):
+            c.bc_kind[q] = int(self.bc_kind[q])
+            c.bc_flip[q] = int(self.bc_flip[q])
+        c.precision = PRECISIONS[self.precision]
+        c.tend = self.tend
+        return c
+
+    @property
+    def shape(self) -> tuple:
+        return (9, self.jx, self.ix) if self.nd == 2 else (9, self.kx, self.jx, self.ix)
+
+    @property
+    def interior_cells(self) -> int:
+        n = (self.ix - 2) * (self.jx - 2)
+        return n * (self.kx - 2) if self.nd == 3 else n
+
+
+@dataclass
+class ModelSpec:
+    kind: int = 0          # 0 Orszag-Tang, 1 KH shear layer, 2 Harris sheet
+    amp: float = 1.0
+    bx0: float = 0.0
+    phase_x: float = 0.0
+    phase_y: float = 0.0
+    beta: float = 0.2
+    pert: float = 0.0
+    seed: int = 0
+
+    def to_c(self) -> _lib.Model:
+        m = _lib.Model()
+        m.kind, m.amp, m.bx0 = self.kind, self.amp, self.bx0
+        m.phase_x, m.phase_y, m.beta, m.pert, m.seed = self.phase_x, self.phase_y, self.beta, self.pert, self.seed
+        return m
+
+
+# ---------------------------------------------------------------------------
+# problem setups
+# ---------------------------------------------------------------------------
+def orszag_tang(nx: int = 256, ny: int | None = None, precision: str = "fp64", limiter: str = "mc",
+                flux: str = "hlld", cfl: float = 0.4, tend: float = math.pi, amp: float = 1.0,
+                phase_x: float = 0.0, phase_y: float = 0.0):
+    """Orszag-Tang vortex on [0,2pi]^2, periodic (2D_basic/model.f90:34-50)."""
+    ny = nx if ny is None else ny
+    two_pi = 2 * (4.0 * math.atan(1.0))
+    cfg = SolverConfig(nd=2, ix=nx + 2, jx=ny + 2, dx=two_pi / nx, dy=two_pi / ny, x0=0.0, y0=0.0,
+                       cfl=cfl, limiter=limiter, flux=flux, precision=precision, tend=tend)
+    if nx == ny:
+        cfg.dy = cfg.dx  # the reference derives y spacing from dx (model.f90:19-28)
+    return cfg, ModelSpec(kind=0, amp=amp, phase_x=phase_x, phase_y=phase_y)
+
+
+def kelvin_helmholtz(nx: int = 4096, ny: int = 2048, precision: str = "fp64", limiter: str = "minmod",
+                     flux: str = "hlld", cfl: float = 0.4, tend: float = 0.0, shear: float = 0.5,
+                     bx0: float = 0.2, pert: float = 0.01, seed: int = 0):
+    """KH shear layer: x in [0,40) periodic, y in [-20,20] with zero-gradient
+    walls; rho=1, p=0.5, vx=shear*tanh(y), Bx=bx0, vy=pert*exp(-y^2)*r(x,y)."""
+    Lx, Ly = 40.0, 40.0
+    cfg = SolverConfig(nd=2, ix=nx + 2, jx=ny + 2, dx=Lx / nx, dy=Ly / ny, x0=0.0, y0=-20.0, cfl=cfl,
+                       limiter=limiter, flux=flux, precision=precision, tend=tend,
+                       bc_kind=(0, 0, 1, 1, 0, 0), bc_flip=(0, 0, 0, 0, 0, 0))
+    if nx == ny:
+        cfg.dy = cfg.dx
+    return cfg, ModelSpec(kind=1, amp=shear, bx0=bx0, pert=pert, seed=seed)
+
+
+def harris3d(nx: int = 512, ny: int = 256, nz: int = 512, precision: str = "fp64", limiter: str = "mc",
+             flux: str = "hlld", cfl: float = 0.4, tend: float = 0.0, beta: float = 0.2, amp: float = 2.0e-3,
+             seed: int = 0):
+    """3D resistive Harris sheet: x in [-100,100], y in [-50,50] periodic, z in
+    [-100,100] conducting walls (mz, Bz flip); eta = 1e-3 + exp(-(x^2+z^2)/4)/60."""
+    dx, dy, dz = 200.0 / nx, 100.0 / ny, 200.0 / nz
+    cfg = SolverConfig(nd=3, ix=nx + 2, jx=ny + 2, kx=nz + 2, dx=dx, dy=dy, dz=dz, x0=-100.0, y0=-50.0,
+                       z0=-100.0, cfl=cfl, limiter=limiter, flux=flux, precision=precision, tend=tend,
+                       eta="harris_xz", bc_kind=(0, 0, 0, 0, 1, 1),
+                       bc_flip=(0, 0, 0, 0, flip(MZ, BZ), flip(MZ, BZ)))
+    if dy == dx:
+        cfg.dy = cfg.dx
+    if dz == dx:
+        cfg.dz = cfg.dx
+    return cfg, ModelSpec(kind=2, beta=beta, amp=amp, seed=seed)
+
+
+# ---------------------------------------------------------------------------
+# solver
+# ---------------------------------------------------------------------------
+class Solver:
+    """Fused TVD-RK2 stepping of one grid on the current CUDA device."""
+
+    def __init__(self, cfg: SolverConfig, stream=None):
+        import torch
+
+        if not torch.cuda.is_available():
+            raise RuntimeError("openmhd_gb300.Solver needs a CUDA device")
+        self.cfg = cfg
+        self.lib = _lib.load()
+        self._h = C.c_void_p()
+        ccfg = cfg.to_c()
+        st = self.lib.omhd_solver_create(C.byref(ccfg), C.byref(self._h))
+        if st:
+            raise OmhdError(st, "omhd_solver_create rejected the configuration")
+        self.stream = stream if stream is not None else torch.cuda.Stream()
+        self.U = torch.empty(cfg.shape, dtype=torch.float64, device="cuda")
+        self.U1 = torch.empty(cfg.shape, dtype=torch.float64, device="cuda")
+        self._check(self.lib.omhd_solver_bind(self._h, self.U.data_ptr(), self.U1.data_ptr()))
+        self._check(self.lib.omhd_solver_set_stream(self._h, C.c_void_p(self.stream.cuda_stream)))
+
+    def _check(self, st: int):
+        if st:
+            info = _lib.ErrorInfo()
+            self.lib.omhd_solver_last_error(self._h, C.byref(info))
+            raise OmhdError(st, info.message.decode(errors="replace"))
+
+    def close(self):
+        if self._h:
+            self.lib.omhd_solver_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state --
+    def init_model(self, m: ModelSpec):
+        import torch
+
+        torch.cuda.current_stream().synchronize()
+        mc = m.to_c()
+        self._check(self.lib.omhd_solver_init_model(self._h, C.byref(mc)))
+        return self
+
+    def put_state(self, U, t: float = 0.0):
+        """Load a full state (numpy array or torch tensor, any device)."""
+        import numpy as np
+        import torch
+
+        if isinstance(U, np.ndarray):
+            a = np.ascontiguousarray(U, dtype=np.float64).reshape(self.cfg.shape)
+            self._check(self.lib.omhd_solver_put_state(self._h, a.ctypes.data, float(t)))
+            self.sync()
+        else:
+            src = U.to(dtype=torch.float64).contiguous().reshape(self.cfg.shape)
+            torch.cuda.current_stream().synchronize()
+            self._check(self.lib.omhd_solver_put_state(self._h, src.data_ptr(), float(t)))
+            self.sync()
+        return self
+
+    def state(self):
+        """The bound state tensor (valid after sync())."""
+        return self.U
+
+    def get_state_numpy(self):
+        import numpy as np
+
+        out = np.empty(self.cfg.shape, dtype=np.float64)
+        self._check(self.lib.omhd_solver_get_state(self._h, out.ctypes.data))
+        return out
+
+    def coords(self):
+        import numpy as np
+
+        x = np.empty(self.cfg.ix)
+        y = np.empty(self.cfg.jx)
+        z = np.empty(self.cfg.kx)
+        self.lib.omhd_solver_coords(self._h, x.ctypes.data, y.ctypes.data, z.ctypes.data)
+        return x, y, z
+
+    # -- stepping --
+    def step(self, n: int = 1):
+        self._check(self.lib.omhd_solver_step(self._h, int(n)))
+        return self
+
+    def step_graph(self, n: int, replays: int = 1):
+        self._check(self.lib.omhd_solver_step_graph(self._h, int(n), int(replays)))
+        return self
+
+    def sync(self) -> _lib.StepInfo:
+        info = _lib.StepInfo()
+        st = self.lib.omhd_solver_sync(self._h, C.byref(info))
+        if st:
+            self._check(st)
+        return info
+
+    def set_tend(self, tend: float):
+        """Set the end time; steps stop on the device at the first t >= tend."""
+        self._check(self.lib.omhd_solver_set_tend(self._h, float(tend)))
+        return self
+
+    def run_until(self, tend: float, batch: int = 64):
+        """Advance until the first t >= tend (main.f90:73).  Steps are enqueued
+        in batches; kernels turn themselves off once t >= tend, so the step
+        count matches the reference's loop exactly."""
+        self.set_tend(tend)
+        while True:
+            self.step(batch)
+            info = self.sync()
+            if info.done:
+                return info
+
+    @property
+    def launches_per_step(self) -> int:
+        return int(self.lib.omhd_solver_launches_per_step(self._h))

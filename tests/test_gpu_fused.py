@@ -1,0 +1,179 @@
+"""Fused-step parity: the GB300 solver (two fused stage kernels per TVD-RK2
+step) against the CPU oracle's restatement of the reference driver loop
+(2D_basic/main.f90:56-188) from the same initial state.
+
+Tolerances (the benchmark spec): FP64 path within 1e-12 relative L1 per variable after
+one step and 1e-9 after N steps; the no-contraction parity build is compared
+at 1e-13 (its only departure from the oracle's op sequence is the device exp()
+in the GLM factor); the FP32-mixed path within 1e-6 relative L1 of FP64."""
+import math
+
+import numpy as np
+import pytest
+
+from helpers import interior, rel_l1
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(cfg, model, oracle_mod):
+    from openmhd_gb300 import Solver
+    from oracle.oracle import Grid
+
+    s = Solver(cfg).init_model(model)
+    g = Grid.from_solver_config(cfg)
+    g.U[...] = s.get_state_numpy()  # identical initial state on both sides
+    return s, g
+
+
+def _cmp(s, g, tol, label=""):
+    U = s.get_state_numpy()
+    err = rel_l1(U, g.U)
+    assert np.all(err <= tol), f"{label} rel L1 per var {err}"
+    return err
+
+
+@pytest.mark.parametrize("precision,tol1,tolN", [("fp64_parity", 1e-13, 1e-12), ("fp64", 1e-12, 1e-9)])
+def test_orszag_tang_vs_oracle(cuda_lib, oracle_mod, precision, tol1, tolN):
+    from openmhd_gb300 import orszag_tang
+
+    cfg, model = orszag_tang(64, precision=precision)
+    s, g = _pair(cfg, model, oracle_mod)
+    s.step(1)
+    info = s.sync()
+    g.step(1)
+    assert info.steps == 1 and info.status == 0
+    assert abs(info.dt - g.last_dt) <= 1e-15 * g.last_dt
+    _cmp(s, g, tol1, "1 step")
+    s.step(9)
+    s.sync()
+    g.step(9)
+    _cmp(s, g, tolN, "10 steps")
+
+
+@pytest.mark.parametrize("flux", ["llf", "hll", "hllc", "hlld", "lhlld"])
+@pytest.mark.parametrize("limiter", ["flat", "minmod", "mc", "vanleer", "koren"])
+def test_scheme_matrix_parity(cuda_lib, oracle_mod, flux, limiter):
+    from openmhd_gb300 import orszag_tang
+
+    cfg, model = orszag_tang(32, 24, precision="fp64_parity", flux=flux, limiter=limiter)
+    s, g = _pair(cfg, model, oracle_mod)
+    s.step(3)
+    s.sync()
+    g.step(3)
+    _cmp(s, g, 1e-13, f"{flux}/{limiter}")
+
+
+@pytest.mark.parametrize("precision", ["fp64_parity", "fp64"])
+def test_kelvin_helmholtz_walls_anisotropic(cuda_lib, oracle_mod, precision):
+    from openmhd_gb300 import kelvin_helmholtz
+
+    cfg, model = kelvin_helmholtz(96, 40, precision=precision)
+    s, g = _pair(cfg, model, oracle_mod)
+    s.step(5)
+    s.sync()
+    g.step(5)
+    _cmp(s, g, 1e-12 if precision == "fp64_parity" else 1e-10, "KH")
+
+
+def test_reconnection_walls_resistive_std_rk2(cuda_lib, oracle_mod):
+    """2D_reconnection-style walls (sign flips on every side) + resistive fluxes
+    (2D_reconnection/flux_resistive.f90) + standard RK2 (rk_std21/22)."""
+    from openmhd_gb300 import ModelSpec, SolverConfig, flip
+    from openmhd_gb300.solver import BX, BY, BZ, MX, MY, MZ, PS
+
+    cfg = SolverConfig(nd=2, ix=50, jx=42, dx=0.25, dy=0.25, x0=-6.0, y0=-5.0, limiter="mc", flux="hlld",
+                       eta="recon2d", time="rk2", precision="fp64_parity",
+                       bc_kind=(1, 1, 1, 1, 0, 0),
+                       bc_flip=(flip(MX, MZ, BY, PS), flip(MX, MZ, BY, PS), flip(MY, MZ, BX, PS), flip(MY, BY), 0, 0))
+    s, g = _pair(cfg, ModelSpec(kind=1, amp=0.3, bx0=0.5, pert=0.05, seed=3), oracle_mod)
+    s.step(4)
+    s.sync()
+    g.step(4)
+    _cmp(s, g, 1e-12, "reconnection")
+
+
+def test_run_until_matches_reference_step_count(cuda_lib, oracle_mod):
+    from openmhd_gb300 import orszag_tang
+
+    cfg, model = orszag_tang(32, precision="fp64")
+    s, g = _pair(cfg, model, oracle_mod)
+    info = s.run_until(0.3, batch=7)
+    g.run_until(0.3)
+    assert info.steps == g.steps and info.done == 1
+    assert abs(info.t - g.t) <= 1e-13
+
+
+def test_conservation_periodic_full_size(cuda_lib):
+    """Mass, momentum and energy totals are conserved to round-off on a periodic
+    grid (size-independent property; 4096^2 Orszag-Tang)."""
+    import torch
+    from openmhd_gb300 import orszag_tang
+
+    cfg, model = orszag_tang(4096, precision="fp64")
+    from openmhd_gb300 import Solver
+
+    s = Solver(cfg).init_model(model)
+    s.sync()
+    tot0 = s.U[:, 1:-1, 1:-1].sum(dim=(1, 2)).cpu().numpy()
+    mag = s.U[:, 1:-1, 1:-1].abs().sum(dim=(1, 2)).cpu().numpy()
+    s.step(3)
+    info = s.sync()
+    assert info.status == 0 and info.steps == 3
+    tot1 = s.U[:, 1:-1, 1:-1].sum(dim=(1, 2)).cpu().numpy()
+    for v in (0, 1, 2, 3, 4):  # mx, my, mz, E, rho
+        assert abs(tot1[v] - tot0[v]) <= 1e-12 * mag[v], (v, tot1[v] - tot0[v])
+    torch.cuda.synchronize()
+
+
+def test_mixed_precision_error_vs_fp64(cuda_lib):
+    from openmhd_gb300 import Solver, kelvin_helmholtz
+
+    cfg64, model = kelvin_helmholtz(256, 128, precision="fp64")
+    cfgmx, _ = kelvin_helmholtz(256, 128, precision="mixed")
+    a = Solver(cfg64).init_model(model)
+    b = Solver(cfgmx).init_model(model)
+    a.step(20)
+    b.step(20)
+    a.sync()
+    b.sync()
+    err = rel_l1(interior(b.get_state_numpy()), interior(a.get_state_numpy()))
+    assert np.all(err[[0, 1, 3, 4, 5]] <= 1e-6), err
+
+
+def test_negative_pressure_is_reported_not_trapped(cuda_lib):
+    from openmhd_gb300 import Solver, orszag_tang
+
+    cfg, model = orszag_tang(32)
+    s = Solver(cfg).init_model(model)
+    U = s.get_state_numpy()
+    U[3, 10, 12] = -5.0  # E < 0 at Fortran (13, 11)
+    s.put_state(U)
+    s.step(2)
+    import ctypes as C
+    from openmhd_gb300 import _lib
+
+    si = _lib.StepInfo()
+    st = s.lib.omhd_solver_sync(s._h, C.byref(si))
+    assert st == 1 and si.status == 1
+    e = _lib.ErrorInfo()
+    s.lib.omhd_solver_last_error(s._h, C.byref(e))
+    assert (e.i, e.j) == (13, 11)
+    assert si.steps == 0  # the state is not advanced past the failure
+    # the context is still usable
+    s.put_state(Solver(cfg).init_model(model).get_state_numpy())
+    s.step(1)
+    assert s.sync().status == 0
+
+
+def test_graph_replay_matches_stream_launches(cuda_lib):
+    from openmhd_gb300 import Solver, orszag_tang
+
+    cfg, model = orszag_tang(128)
+    a = Solver(cfg).init_model(model)
+    b = Solver(cfg).init_model(model)
+    a.step(8)
+    b.step_graph(4, replays=2)
+    ia, ib = a.sync(), b.sync()
+    assert ia.steps == ib.steps == 8
+    assert np.array_equal(a.get_state_numpy(), b.get_state_numpy())
