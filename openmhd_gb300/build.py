@@ -29,7 +29,9 @@ UNITS = {
     "omhd_fused2d_fp64.cu": ["--fmad=true"],
     "omhd_fused2d_parity.cu": ["--fmad=false"],
     "omhd_fused2d_mixed.cu": ["--fmad=true"],
-    "omhd_fused3d_stub.cu": [],
+    "omhd_fused3d_fp64.cu": ["--fmad=true"],
+    "omhd_fused3d_parity.cu": ["--fmad=false"],
+    "omhd_fused3d_mixed.cu": ["--fmad=true"],
 }
 
 

@@ -99,7 +99,8 @@ __global__ void __launch_bounds__(NT) k_stage2d(const StageArgs a) {
     const double* U = a.Uin;
     const double ro = U[RO * N + c];
     const double mx = U[MX * N + c], my = U[MY * N + c], mz = U[MZ * N + c];
-    const double vx = mx / ro, vy = my / ro, vz = mz / ro;  // u2v.f90:24
+    const double vx = div_<double, OMHD_FAST>(mx, ro), vy = div_<double, OMHD_FAST>(my, ro),
+                 vz = div_<double, OMHD_FAST>(mz, ro);  // u2v.f90:24
     const double rv2 = vx * mx + vy * my + vz * mz;
     const double bx = U[BX * N + c], by = U[BY * N + c], bz = U[BZ * N + c];
     const double B2 = bx * bx + by * by + bz * bz;
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(NT) k_stage2d(const StageArgs a) {
       L[v] = SL[v * SFACE + cy * XS + fx];
       R[v] = SR[v * SFACE + cy * XS + fx + 1];
     }
-    riemann_flux<T, 1, FLUX>(L, R, ch, gam, r1, r2, Fo);
+    riemann_flux<T, 1, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
     if (resist) {  // 2D_reconnection/flux_resistive.f90:266-283
       const int g = gi0 - 1 + fx, gj = gj0 + cy;
       if (g >= 0 && g <= ix - 2 && gj <= jx - 2) {
@@ -233,7 +234,7 @@ __global__ void __launch_bounds__(NT) k_stage2d(const StageArgs a) {
       L[v] = SL[v * SFACE + fy * TX + cx];
       R[v] = SR[v * SFACE + (fy + 1) * TX + cx];
     }
-    riemann_flux<T, 2, FLUX>(L, R, ch, gam, r1, r2, Fo);
+    riemann_flux<T, 2, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
     if (resist) {  // 2D_reconnection/flux_resistive.f90:289-306
       const int gi = gi0 + cx, g = gj0 - 1 + fy;
       if (g >= 0 && g <= jx - 2 && gi <= ix - 2) {
@@ -296,13 +297,13 @@ __global__ void __launch_bounds__(NT) k_stage2d(const StageArgs a) {
 
     if (a.stage == 2) {  // set_dt.f90:27-37 on the new state
       const double ro = out[RO];
-      const double vx = out[MX] / ro, vy = out[MY] / ro, vz = out[MZ] / ro;
+      const double vx = div_<double, OMHD_FAST>(out[MX], ro), vy = div_<double, OMHD_FAST>(out[MY], ro), vz = div_<double, OMHD_FAST>(out[MZ], ro);
       const double rv2 = vx * out[MX] + vy * out[MY] + vz * out[MZ];
       const double B2 = out[BX] * out[BX] + out[BY] * out[BY] + out[BZ] * out[BZ];
       const double pr = f1g * (out[EN] - 0.5 * (rv2 + B2));
       const double f1 = gamma * pr;
-      const double vfx = fast_speed(f1, B2, out[BX], ro);
-      const double vfy = fast_speed(f1, B2, out[BY], ro);
+      const double vfx = fast_speed<double, OMHD_FAST>(f1, B2, out[BX], ro);
+      const double vfy = fast_speed<double, OMHD_FAST>(f1, B2, out[BY], ro);
       vcell = fmax2(fabs(vx) + vfx, fabs(vy) + vfy);
     }
   }

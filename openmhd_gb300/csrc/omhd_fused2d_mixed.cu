@@ -1,6 +1,7 @@
 // omhd_fused2d_mixed.cu -- 2D fused stage kernels, arithmetic variant "mixed"
 // (face arithmetic in float).
 #define OMHD_VARIANT v_mixed
+#define OMHD_FAST true
 #include "omhd_fused2d.cuh"
 
 namespace omhd {

@@ -1,6 +1,7 @@
 // omhd_fused2d_parity.cu -- 2D fused stage kernels, arithmetic variant "parity"
 // (face arithmetic in double; built with --fmad=false so the op sequence is the reference's).
 #define OMHD_VARIANT v_parity
+#define OMHD_FAST false
 #include "omhd_fused2d.cuh"
 
 namespace omhd {

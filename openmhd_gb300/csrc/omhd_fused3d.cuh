@@ -1,0 +1,455 @@
+// omhd_fused3d.cuh -- one fused kernel per TVD-RK2 stage for 3D grids.
+//
+// A CTA owns a TX x TY column of interior cells and marches it through a
+// chunk of z planes.  A ring of four primitive planes (k-1 .. k+2, each with
+// a two-cell x/y halo) lives in shared memory, so the conserved->primitive
+// recovery of every plane is done once per CTA; per plane the CTA
+//   - loads and converts plane k+2 (u2v.f90, first GLM half in stage 1),
+//   - builds x and y face states and fluxes of plane k in shared memory
+//     (limiter.f90, flux_solver.f90, bc_for_F/G face fixes),
+//   - reconstructs cell k+1 in z and solves the z face k+1/2 in registers,
+//     carrying the z flux of face k-1/2 from the previous plane,
+//   - updates plane k (rk.f90), fills ghosts by owner writes (bc),
+//     applies the second GLM half and the CFL reduction in stage 2.
+// Resistive fluxes (3D_reconnection_gpu/flux_resistive.cuf) are added at
+// each face from cell-centred B in the ring.
+#pragma once
+#include "omhd_fused.h"
+#include "omhd_step.cuh"
+
+#ifndef OMHD_VARIANT
+#error "define OMHD_VARIANT before including omhd_fused3d.cuh"
+#endif
+
+namespace omhd {
+namespace OMHD_VARIANT {
+namespace d3 {
+
+constexpr int TX = 32, TY = 8, NT = TX * TY;
+constexpr int RX = TX + 4, RY = TY + 4, PL = RX * RY;  // plane of the halo tile
+constexpr int NRING = 4;
+constexpr int SFACE = (TY * (TX + 2) > (TY + 2) * TX) ? TY * (TX + 2) : (TY + 2) * TX;
+constexpr int SFLUX = (TY * (TX + 1) > (TY + 1) * TX) ? TY * (TX + 1) : (TY + 1) * TX;
+constexpr int ZCHUNK = 64;  // z planes marched by one CTA
+
+template <class T>
+constexpr size_t smem3d_bytes() {
+  return sizeof(T) * (size_t)NV * (NRING * PL + 2 * SFACE + SFLUX);
+}
+
+__device__ __forceinline__ int map_idx(int g, int n, bool periodic) {
+  if (g >= 0 && g < n) return g;
+  if (periodic) {
+    const int P = n - 2;
+    int r = (g - 1) % P;
+    if (r < 0) r += P;
+    return r + 1;
+  }
+  return g < 0 ? 0 : n - 1;
+}
+
+__device__ __forceinline__ double eta3(int kind, double x, double y, double z) {
+  if (kind == OMHD_ETA_RECON2D) {  // 2D_reconnection/flux_resistive.f90:1-16 (as coded in the 3D GPU driver)
+    const double Rm1 = 60.0, Rm0 = 1000.0;
+    const double eta0 = 1.0 / Rm0;
+    const double eta01 = (Rm0 - Rm1) / (Rm0 * Rm1);
+    const double c = cosh(fmin2(sqrt(x * x + y * y), 25.0));
+    return eta0 + eta01 * (1.0 / (c * c));
+  }
+  if (kind == OMHD_ETA_HARRIS_XZ) return 1.0e-3 + (1.0 / 60.0) * exp(-(x * x + z * z) / 4.0);
+  return 0.0;
+}
+
+// Load + convert one z plane (global index gk, any value; mapped by the z bc)
+// of the halo tile into ring slot `slot`.
+template <class T>
+__device__ __forceinline__ void load_plane(const StageArgs& a, T* W, int slot, int gk, int gi0, int gj0, bool perx,
+                                           bool pery, bool perz, bool resist, double glmf, bool own_plane) {
+  const int ix = a.ix, jx = a.jx, kx = a.kx;
+  const size_t N = (size_t)ix * jx * kx;
+  const double f1g = a.gamma - 1;
+  const int mk = map_idx(gk, kx, perz);
+  T* Ws = W + (size_t)slot * NV * PL;
+  for (int q = threadIdx.x; q < PL; q += NT) {
+    const int rx = q % RX, ry = q / RX;
+    const bool cx_in = rx >= 2 && rx < TX + 2, cy_in = ry >= 2 && ry < TY + 2;
+    if (!cx_in && !cy_in) {
+      if (!resist || rx == 0 || rx == RX - 1 || ry == 0 || ry == RY - 1) continue;
+    }
+    const int gi = gi0 - 2 + rx, gj = gj0 - 2 + ry;
+    const size_t c = (size_t)map_idx(gi, ix, perx) + (size_t)ix * ((size_t)map_idx(gj, jx, pery) + (size_t)jx * mk);
+    const double* U = a.Uin;
+    const double ro = U[RO * N + c];
+    const double mx = U[MX * N + c], my = U[MY * N + c], mz = U[MZ * N + c];
+    const double vx = div_<double, OMHD_FAST>(mx, ro), vy = div_<double, OMHD_FAST>(my, ro),
+                 vz = div_<double, OMHD_FAST>(mz, ro);  // 3D_basic/u2v.f90:24
+    const double rv2 = vx * mx + vy * my + vz * mz;
+    const double bx = U[BX * N + c], by = U[BY * N + c], bz = U[BZ * N + c];
+    const double B2 = bx * bx + by * by + bz * bz;
+    const double pr = f1g * (U[EN * N + c] - 0.5 * (rv2 + B2));
+    double ps = U[PS * N + c];
+    if (a.stage == 1) ps = glmf * ps;
+    Ws[VX * PL + q] = T(vx);
+    Ws[VY * PL + q] = T(vy);
+    Ws[VZ * PL + q] = T(vz);
+    Ws[PR * PL + q] = T(pr);
+    Ws[RO * PL + q] = T(ro);
+    Ws[BX * PL + q] = T(bx);
+    Ws[BY * PL + q] = T(by);
+    Ws[BZ * PL + q] = T(bz);
+    Ws[PS * PL + q] = T(ps);
+    if (own_plane && cx_in && cy_in && gi <= ix - 2 && gj <= jx - 2) {  // u2v.f90:36-45, owner check
+      if (pr <= 0)
+        raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, gk + 1, 0, pr);
+      else if (ro <= 0)
+        raise_error(a.err, OMHD_NEG_DENSITY, gi + 1, gj + 1, gk + 1, 0, ro);
+    }
+  }
+}
+
+template <class T, int FLUX>
+__global__ void __launch_bounds__(NT) k_stage3d(const StageArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* W = reinterpret_cast<T*>(smem_raw);  // [NRING][NV][PL]
+  T* SL = W + NRING * NV * PL;
+  T* SR = SL + NV * SFACE;
+  T* FB = SR + NV * SFACE;
+  __shared__ double red32[32];
+
+  StepState* st = a.st;
+  if (st->done || *(volatile int*)&a.err->code) return;
+  const double dt = st->dt, chd = st->ch, glmf = st->glm_f;
+  const int ix = a.ix, jx = a.jx, kx = a.kx;
+  const size_t N = (size_t)ix * jx * kx;
+  const int tid = threadIdx.x;
+  const int gi0 = 1 + blockIdx.x * TX, gj0 = 1 + blockIdx.y * TY;
+  const int k0 = 1 + blockIdx.z * ZCHUNK;
+  const int k1 = min(k0 + ZCHUNK - 1, kx - 2);
+  const bool perx = a.bc_kind[0] == OMHD_BC_PERIODIC, pery = a.bc_kind[2] == OMHD_BC_PERIODIC;
+  const bool perz = a.bc_kind[4] == OMHD_BC_PERIODIC;
+  const bool resist = a.eta_kind != OMHD_ETA_NONE;
+  const double gamma = a.gamma;
+  const double f1g = gamma - 1;
+  const T ch = T(chd), gam = T(gamma);
+  const T r1 = T(1.0 / (gamma - 1.0)), r2 = T(gamma / (gamma - 1.0));
+  const int lm = a.lm_type;
+  const int tx = tid % TX, ty = tid / TX;
+  const int gi = gi0 + tx, gj = gj0 + ty;
+  const bool own = gi <= ix - 2 && gj <= jx - 2;
+  const int oc = (ty + 2) * RX + (tx + 2);  // own column in a ring plane
+  const double dtx = a.dtx_scale * dt / a.dx, dty = a.dtx_scale * dt / a.dy, dtz = a.dtx_scale * dt / a.dz;
+  auto slot = [](int k) { return ((k % NRING) + NRING) % NRING; };
+  auto Wv = [&](int k, int v, int o) -> T { return W[(size_t)slot(k) * NV * PL + v * PL + o]; };
+
+  // ---- prologue: planes k0-2 .. k0+1, z face k0-1/2, cached upper state of cell k0 ----
+  for (int p = k0 - 2; p <= k0 + 1; ++p)
+    load_plane<T>(a, W, slot(p), p, gi0, gj0, perx, pery, perz, resist, glmf, p == k0);
+  __syncthreads();
+  T sLc[NV];  // z-upper face state of the current cell (k)
+  double Fzp[NV];  // z flux through face k-1/2
+  {
+    T L[NV], R[NV], Fo[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      T l, r;
+      reconstruct<T>(lm, Wv(k0 - 2, v, oc), Wv(k0 - 1, v, oc), Wv(k0, v, oc), l, r);
+      L[v] = l;  // upper state of cell k0-1
+      reconstruct<T>(lm, Wv(k0 - 1, v, oc), Wv(k0, v, oc), Wv(k0 + 1, v, oc), l, r);
+      R[v] = r;  // lower state of cell k0
+      sLc[v] = l;
+    }
+    if (!perz && k0 == 1) {  // bottom wall: VL = flip(VR)  (3D_reconnection_gpu/bc.cuf bc_for_H pattern)
+#pragma unroll
+      for (int v = 0; v < NV; ++v) L[v] = ((a.bc_flip[4] >> v) & 1) ? -R[v] : R[v];
+    }
+    riemann_flux<T, 3, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) Fzp[v] = double(Fo[v]);
+    if (resist && own) {  // z face k0-1/2 (flux_resistive.cuf:121-135)
+      const int k = k0 - 1;
+      auto B = [&](int var, int dxo, int dyo, int dzo) { return double(Wv(k + dzo, var, oc + dxo + dyo * RX)); };
+      const double eta_dx = eta3(a.eta_kind, a.xc[gi], a.yc[gj], a.zc[k] + 0.5 * a.dx) / a.dx;
+      const double JyS = (B(BX, 0, 0, 1) - B(BX, 0, 0, 0)) -
+                         0.25 * (B(BZ, 1, 0, 0) + B(BZ, 1, 0, 1) - B(BZ, -1, 0, 0) - B(BZ, -1, 0, 1));
+      const double JxS = -(B(BY, 0, 0, 1) - B(BY, 0, 0, 0)) +
+                         0.25 * (B(BZ, 0, 1, 0) + B(BZ, 0, 1, 1) - B(BZ, 0, -1, 0) - B(BZ, 0, -1, 1));
+      Fzp[EN] = Fzp[EN] + 0.5 * eta_dx * (JxS * (B(BY, 0, 0, 0) + B(BY, 0, 0, 1)) - JyS * (B(BX, 0, 0, 0) + B(BX, 0, 0, 1)));
+      Fzp[BX] = Fzp[BX] - eta_dx * JyS;
+      Fzp[BY] = Fzp[BY] + eta_dx * JxS;
+      if (sizeof(T) == 4) {  // keep the face value the mixed build would round to
+#pragma unroll
+        for (int v = 0; v < NV; ++v) Fzp[v] = double(T(Fzp[v]));
+      }
+    }
+  }
+  double vloc = 0.0;
+
+  for (int k = k0; k <= k1; ++k) {
+    __syncthreads();  // ring slot of plane k-2 is free
+    load_plane<T>(a, W, slot(k + 2), k + 2, gi0, gj0, perx, pery, perz, resist, glmf, false);
+    __syncthreads();
+    if (k > k0) {
+      // positivity of the current plane's own cells (u2v.f90:36-45); plane k0
+      // was checked at load time in the prologue
+      if (own) {
+        const double ro = double(Wv(k, RO, oc)), pr = double(Wv(k, PR, oc));
+        if (pr <= 0)
+          raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, k + 1, 0, pr);
+        else if (ro <= 0)
+          raise_error(a.err, OMHD_NEG_DENSITY, gi + 1, gj + 1, k + 1, 0, ro);
+      }
+    }
+    const T* Wk = W + (size_t)slot(k) * NV * PL;
+
+    // ---- x pass on plane k ----
+    constexpr int XS = TX + 2;
+    for (int q = tid; q < TY * XS; q += NT) {
+      const int cx = q % XS, cy = q / XS;
+      const int o = (cy + 2) * RX + (cx + 1);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        T l, r;
+        reconstruct<T>(lm, Wk[v * PL + o - 1], Wk[v * PL + o], Wk[v * PL + o + 1], l, r);
+        SL[v * SFACE + q] = l;
+        SR[v * SFACE + q] = r;
+      }
+    }
+    __syncthreads();
+    if (!perx) {
+      if (gi0 == 1 && tid < TY * NV) {
+        const int cy = tid % TY, v = tid / TY;
+        const T s = SR[v * SFACE + cy * XS + 1];
+        SL[v * SFACE + cy * XS + 0] = ((a.bc_flip[0] >> v) & 1) ? -s : s;
+      }
+      const int cl = (ix - 2) - gi0 + 1;
+      if (cl >= 1 && cl <= TX && tid < TY * NV) {
+        const int cy = tid % TY, v = tid / TY;
+        const T s = SL[v * SFACE + cy * XS + cl];
+        SR[v * SFACE + cy * XS + cl + 1] = ((a.bc_flip[1] >> v) & 1) ? -s : s;
+      }
+      __syncthreads();
+    }
+    constexpr int XF = TX + 1;
+    for (int q = tid; q < TY * XF; q += NT) {
+      const int fx = q % XF, cy = q / XF;
+      T L[NV], R[NV], Fo[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        L[v] = SL[v * SFACE + cy * XS + fx];
+        R[v] = SR[v * SFACE + cy * XS + fx + 1];
+      }
+      riemann_flux<T, 1, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
+      if (resist) {  // flux_resistive.cuf:87-101
+        const int g = gi0 - 1 + fx, gjj = gj0 + cy;
+        if (g >= 0 && g <= ix - 2 && gjj <= jx - 2) {
+          const int o = (cy + 2) * RX + (fx + 1);
+          auto B = [&](int var, int dxo, int dyo, int dzo) { return double(Wv(k + dzo, var, o + dxo + dyo * RX)); };
+          const double eta_dx = eta3(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gjj], a.zc[k]) / a.dx;
+          const double JyS = -(B(BZ, 1, 0, 0) - B(BZ, 0, 0, 0)) +
+                             0.25 * (B(BX, 0, 0, 1) + B(BX, 1, 0, 1) - B(BX, 0, 0, -1) - B(BX, 1, 0, -1));
+          const double JzS = (B(BY, 1, 0, 0) - B(BY, 0, 0, 0)) -
+                             0.25 * (B(BX, 0, 1, 0) + B(BX, 1, 1, 0) - B(BX, 0, -1, 0) - B(BX, 1, -1, 0));
+          Fo[EN] = T(double(Fo[EN]) + 0.5 * eta_dx * (JyS * (B(BZ, 0, 0, 0) + B(BZ, 1, 0, 0)) - JzS * (B(BY, 0, 0, 0) + B(BY, 1, 0, 0))));
+          Fo[BY] = T(double(Fo[BY]) - eta_dx * JzS);
+          Fo[BZ] = T(double(Fo[BZ]) + eta_dx * JyS);
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < NV; ++v) FB[v * SFLUX + q] = Fo[v];
+    }
+    __syncthreads();
+    double acc[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      acc[v] = double(FB[v * SFLUX + ty * XF + tx]) - double(FB[v * SFLUX + ty * XF + tx + 1]);
+    __syncthreads();
+
+    // ---- y pass on plane k ----
+    for (int q = tid; q < (TY + 2) * TX; q += NT) {
+      const int cx = q % TX, cy = q / TX;
+      const int o = (cy + 1) * RX + (cx + 2);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        T l, r;
+        reconstruct<T>(lm, Wk[v * PL + o - RX], Wk[v * PL + o], Wk[v * PL + o + RX], l, r);
+        SL[v * SFACE + q] = l;
+        SR[v * SFACE + q] = r;
+      }
+    }
+    __syncthreads();
+    if (!pery) {
+      if (gj0 == 1 && tid < TX) {
+        for (int v = 0; v < NV; ++v) {
+          const T s = SR[v * SFACE + 1 * TX + tid];
+          SL[v * SFACE + 0 * TX + tid] = ((a.bc_flip[2] >> v) & 1) ? -s : s;
+        }
+      }
+      const int cl = (jx - 2) - gj0 + 1;
+      if (cl >= 1 && cl <= TY && tid < TX) {
+        for (int v = 0; v < NV; ++v) {
+          const T s = SL[v * SFACE + cl * TX + tid];
+          SR[v * SFACE + (cl + 1) * TX + tid] = ((a.bc_flip[3] >> v) & 1) ? -s : s;
+        }
+      }
+      __syncthreads();
+    }
+    for (int q = tid; q < (TY + 1) * TX; q += NT) {
+      const int cx = q % TX, fy = q / TX;
+      T L[NV], R[NV], Fo[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        L[v] = SL[v * SFACE + fy * TX + cx];
+        R[v] = SR[v * SFACE + (fy + 1) * TX + cx];
+      }
+      riemann_flux<T, 2, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
+      if (resist) {  // flux_resistive.cuf:104-118
+        const int gii = gi0 + cx, g = gj0 - 1 + fy;
+        if (g >= 0 && g <= jx - 2 && gii <= ix - 2) {
+          const int o = (fy + 1) * RX + (cx + 2);
+          auto B = [&](int var, int dxo, int dyo, int dzo) { return double(Wv(k + dzo, var, o + dxo + dyo * RX)); };
+          const double eta_dx = eta3(a.eta_kind, a.xc[gii], a.yc[g] + 0.5 * a.dx, a.zc[k]) / a.dx;
+          const double JxS = (B(BZ, 0, 1, 0) - B(BZ, 0, 0, 0)) -
+                             0.25 * (B(BY, 0, 0, 1) + B(BY, 0, 1, 1) - B(BY, 0, 0, -1) - B(BY, 0, 1, -1));
+          const double JzS = -(B(BX, 0, 1, 0) - B(BX, 0, 0, 0)) +
+                             0.25 * (B(BY, 1, 0, 0) + B(BY, 1, 1, 0) - B(BY, -1, 0, 0) - B(BY, -1, 1, 0));
+          Fo[EN] = T(double(Fo[EN]) + 0.5 * eta_dx * (JzS * (B(BX, 0, 0, 0) + B(BX, 0, 1, 0)) - JxS * (B(BZ, 0, 0, 0) + B(BZ, 0, 1, 0))));
+          Fo[BX] = T(double(Fo[BX]) + eta_dx * JzS);
+          Fo[BZ] = T(double(Fo[BZ]) - eta_dx * JxS);
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < NV; ++v) FB[v * SFLUX + q] = Fo[v];
+    }
+    __syncthreads();
+    double gm[NV], gp[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      gm[v] = double(FB[v * SFLUX + ty * TX + tx]);
+      gp[v] = double(FB[v * SFLUX + (ty + 1) * TX + tx]);
+    }
+
+    // ---- z face k+1/2 in registers ----
+    double Fzc[NV];
+    T sLn[NV];
+    {
+      T L[NV], R[NV], Fo[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        T l, r;
+        reconstruct<T>(lm, Wv(k, v, oc), Wv(k + 1, v, oc), Wv(k + 2, v, oc), l, r);
+        L[v] = sLc[v];
+        R[v] = r;
+        sLn[v] = l;
+      }
+      if (!perz && k == kx - 2) {  // top wall: VR = flip(VL)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) R[v] = ((a.bc_flip[5] >> v) & 1) ? -L[v] : L[v];
+      }
+      riemann_flux<T, 3, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) Fzc[v] = double(Fo[v]);
+      if (resist && own) {  // flux_resistive.cuf:121-135
+        auto B = [&](int var, int dxo, int dyo, int dzo) { return double(Wv(k + dzo, var, oc + dxo + dyo * RX)); };
+        const double eta_dx = eta3(a.eta_kind, a.xc[gi], a.yc[gj], a.zc[k] + 0.5 * a.dx) / a.dx;
+        const double JyS = (B(BX, 0, 0, 1) - B(BX, 0, 0, 0)) -
+                           0.25 * (B(BZ, 1, 0, 0) + B(BZ, 1, 0, 1) - B(BZ, -1, 0, 0) - B(BZ, -1, 0, 1));
+        const double JxS = -(B(BY, 0, 0, 1) - B(BY, 0, 0, 0)) +
+                           0.25 * (B(BZ, 0, 1, 0) + B(BZ, 0, 1, 1) - B(BZ, 0, -1, 0) - B(BZ, 0, -1, 1));
+        Fzc[EN] = Fzc[EN] + 0.5 * eta_dx * (JxS * (B(BY, 0, 0, 0) + B(BY, 0, 0, 1)) - JyS * (B(BX, 0, 0, 0) + B(BX, 0, 0, 1)));
+        Fzc[BX] = Fzc[BX] - eta_dx * JyS;
+        Fzc[BY] = Fzc[BY] + eta_dx * JxS;
+        if (sizeof(T) == 4) {
+#pragma unroll
+          for (int v = 0; v < NV; ++v) Fzc[v] = double(T(Fzc[v]));
+        }
+      }
+    }
+
+    // ---- update plane k ----
+    if (own) {
+      const size_t c = (size_t)gi + (size_t)ix * ((size_t)gj + (size_t)jx * k);
+      double out[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double d;
+        if (a.iso)
+          d = dtx * (acc[v] + gm[v] - gp[v] + Fzp[v] - Fzc[v]);  // 3D_basic/rk.f90:26-35 order
+        else
+          d = dtx * acc[v] + dty * (gm[v] - gp[v]) + dtz * (Fzp[v] - Fzc[v]);
+        double ub = a.Ubase[v * N + c];
+        if (v == PS) ub = glmf * ub;
+        if (a.stage == 1 || a.time_type == OMHD_TIME_RK2)
+          out[v] = ub + d;
+        else
+          out[v] = 0.5 * (ub + a.U1[v * N + c] + d);
+      }
+      if (a.stage == 2) out[PS] = glmf * out[PS];
+      int xt[3], yt[3], zt[3], xf[3], yf[3], zf[3], nxt = 1, nyt = 1, nzt = 1;
+      xt[0] = gi; xf[0] = 0; yt[0] = gj; yf[0] = 0; zt[0] = k; zf[0] = 0;
+      if (gi == 1) { xt[nxt] = perx ? ix - 1 : 0; xf[nxt] = perx ? 0 : a.bc_flip[0]; ++nxt; }
+      if (gi == ix - 2) { xt[nxt] = perx ? 0 : ix - 1; xf[nxt] = perx ? 0 : a.bc_flip[1]; ++nxt; }
+      if (gj == 1) { yt[nyt] = pery ? jx - 1 : 0; yf[nyt] = pery ? 0 : a.bc_flip[2]; ++nyt; }
+      if (gj == jx - 2) { yt[nyt] = pery ? 0 : jx - 1; yf[nyt] = pery ? 0 : a.bc_flip[3]; ++nyt; }
+      if (k == 1) { zt[nzt] = perz ? kx - 1 : 0; zf[nzt] = perz ? 0 : a.bc_flip[4]; ++nzt; }
+      if (k == kx - 2) { zt[nzt] = perz ? 0 : kx - 1; zf[nzt] = perz ? 0 : a.bc_flip[5]; ++nzt; }
+      for (int e = 0; e < nzt; ++e)
+        for (int b = 0; b < nyt; ++b)
+          for (int q = 0; q < nxt; ++q) {
+            const size_t cc = (size_t)xt[q] + (size_t)ix * ((size_t)yt[b] + (size_t)jx * zt[e]);
+            const int fm = xf[q] ^ yf[b] ^ zf[e];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) a.Uout[v * N + cc] = ((fm >> v) & 1) ? -out[v] : out[v];
+          }
+      if (a.stage == 2) {  // 3D_basic/set_dt.f90:27-43 on the new state
+        const double ro = out[RO];
+        const double vx = div_<double, OMHD_FAST>(out[MX], ro), vy = div_<double, OMHD_FAST>(out[MY], ro), vz = div_<double, OMHD_FAST>(out[MZ], ro);
+        const double rv2 = vx * out[MX] + vy * out[MY] + vz * out[MZ];
+        const double B2 = out[BX] * out[BX] + out[BY] * out[BY] + out[BZ] * out[BZ];
+        const double pr = f1g * (out[EN] - 0.5 * (rv2 + B2));
+        const double f1 = gamma * pr;
+        double s = fmax2(fabs(vx) + fast_speed<double, OMHD_FAST>(f1, B2, out[BX], ro), fabs(vy) + fast_speed<double, OMHD_FAST>(f1, B2, out[BY], ro));
+        s = fmax2(s, fabs(vz) + fast_speed<double, OMHD_FAST>(f1, B2, out[BZ], ro));
+        vloc = fmax2(s, vloc);
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      Fzp[v] = Fzc[v];
+      sLc[v] = sLn[v];
+    }
+  }
+  if (a.stage == 2) {
+    const double bm = block_max_pos(vloc, red32);
+    StepConsts sc{a.cfl, a.dmin, a.dx, a.eta_kind};
+    reduce_and_finalize(st, sc, a.err, bm, gridDim.x * gridDim.y * gridDim.z, 1);
+  }
+}
+
+template <class T, int FLUX>
+int launch_one3d(const StageArgs& a, cudaStream_t s) {
+  const size_t bytes = smem3d_bytes<T>();
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_stage3d<T, FLUX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return (int)e;
+    configured = true;
+  }
+  dim3 grid((a.ix - 2 + TX - 1) / TX, (a.jx - 2 + TY - 1) / TY, (a.kx - 2 + ZCHUNK - 1) / ZCHUNK);
+  k_stage3d<T, FLUX><<<grid, NT, bytes, s>>>(a);
+  return (int)cudaGetLastError();
+}
+
+template <class T>
+int launch_variant3d(const StageArgs& a, cudaStream_t s) {
+  switch (a.flux_type) {
+    case FX_LLF: return launch_one3d<T, FX_LLF>(a, s);
+    case FX_HLL: return launch_one3d<T, FX_HLL>(a, s);
+    case FX_HLLC: return launch_one3d<T, FX_HLLC>(a, s);
+    case FX_HLLD: return launch_one3d<T, FX_HLLD>(a, s);
+    default: return launch_one3d<T, FX_LHLLD>(a, s);
+  }
+}
+
+}  // namespace d3
+}  // namespace OMHD_VARIANT
+}  // namespace omhd

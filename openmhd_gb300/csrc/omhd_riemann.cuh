@@ -14,6 +14,51 @@
 
 namespace omhd {
 
+// ---------------------------------------------------------------------------
+// FP64 division and square root on a GPU whose FP64 pipe issues ~0.5 T
+// instructions/s: an IEEE divide costs ~8.5 FP64-pipe instructions and a
+// square root ~10.  The performance variants (FAST = true) replace them by
+// Newton-Raphson iterations (Newton's method for f(y) = 1/y - x and
+// f(y) = 1/y^2 - x, quadratic convergence) started from hardware
+// approximations: rcp.approx.ftz.f64 (the special-function unit, ~20 bits)
+// and rsqrt.approx.ftz.f32 on the float-rounded argument (~22 bits).  Two
+// iterations give ~1 ulp; one reciprocal or one rsqrt is shared by every use
+// of the same denominator.  The parity variant (FAST = false) keeps the
+// reference's IEEE operations.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double rcp_nr(double x) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  double e = fma(-x, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-x, y, 1.0);
+  return fma(y, e, y);
+}
+
+__device__ __forceinline__ double rsqrt_nr(double x) {
+  const float xf = (float)x;
+  if (!(xf > 1.0e-37f && xf < 1.0e37f)) return 1.0 / sqrt(x);  // outside the float seed's range
+  float y0;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y0) : "f"(xf));
+  double y = (double)y0;
+  double e = fma(-x * y, y, 1.0);
+  y = fma(0.5 * y, e, y);
+  e = fma(-x * y, y, 1.0);
+  return fma(0.5 * y, e, y);
+}
+
+// a / b and 1 / b under the variant's policy
+template <class T, bool FAST>
+__device__ __forceinline__ T rcp_(T b) {
+  if constexpr (FAST && sizeof(T) == 8) return rcp_nr(b);
+  return T(1) / b;
+}
+template <class T, bool FAST>
+__device__ __forceinline__ T div_(T a, T b) {
+  if constexpr (FAST && sizeof(T) == 8) return a * rcp_nr(b);
+  return a / b;
+}
+
 enum { LM_FLAT = 0, LM_MINMOD = 1, LM_MC = 2, LM_VANLEER = 3, LM_KOREN = 4 };
 enum { FX_LLF = 0, FX_HLL = 1, FX_HLLC = 2, FX_HLLD = 3, FX_LHLLD = 4 };
 
@@ -65,7 +110,7 @@ __device__ __forceinline__ void reconstruct(int type, T wm, T w0, T wp, T& left,
 //   LLF :89-148, HLL :153-221, HLLC :226-347, HLLD :352-585 (HLLC-G fallback
 //   :447-476), LHLLD :590-789; GLM fluxes for Bn and psi :580-581.
 // r1 = 1/(gamma-1), r2 = gamma/(gamma-1) are passed in (flux_solver.f90:38-39).
-template <class T, int DIR, int TYPE>
+template <class T, int DIR, int TYPE, bool FAST = false>
 __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV], T ch, T gamma, T r1,
                                              T r2, T (&Fo)[NV]) {
   constexpr int vn = VX + (DIR - 1) % 3, vt1 = VX + DIR % 3, vt2 = VX + (DIR + 1) % 3;
@@ -101,13 +146,13 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   f1 = gamma * L[PR];
   f2 = 4 * (L[bn] * L[bn]);
   if (TYPE == FX_LLF) {
-    aL = sqrt(((f1 + B2) + sqrt((f1 + B2) * (f1 + B2) - f1 * f2)) / (2 * L[RO]));
+    aL = sqrt(div_<T, FAST>((f1 + B2) + sqrt((f1 + B2) * (f1 + B2) - f1 * f2), 2 * L[RO]));
   } else {
-    aL = ((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f1 * f2, T(0)))) / (2 * L[RO]);
+    aL = div_<T, FAST>((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f1 * f2, T(0))), 2 * L[RO]);
     ptL = L[PR] + T(0.5) * B2;
     if (TYPE == FX_LHLLD) {
       const T g1 = L[RO] * v2;
-      aL1 = ((g1 + B2) + sqrt(fmax2((g1 + B2) * (g1 + B2) - g1 * f2, T(0)))) / (2 * L[RO]);
+      aL1 = div_<T, FAST>((g1 + B2) + sqrt(fmax2((g1 + B2) * (g1 + B2) - g1 * f2, T(0))), 2 * L[RO]);
     }
   }
 
@@ -129,13 +174,13 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   f1 = gamma * R[PR];
   f2 = 4 * (R[bn] * R[bn]);
   if (TYPE == FX_LLF) {
-    aR = sqrt(((f1 + B2) + sqrt((f1 + B2) * (f1 + B2) - f1 * f2)) / (2 * R[RO]));
+    aR = sqrt(div_<T, FAST>((f1 + B2) + sqrt((f1 + B2) * (f1 + B2) - f1 * f2), 2 * R[RO]));
   } else {
-    aR = ((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f1 * f2, T(0)))) / (2 * R[RO]);
+    aR = div_<T, FAST>((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f1 * f2, T(0))), 2 * R[RO]);
     ptR = R[PR] + T(0.5) * B2;
     if (TYPE == FX_LHLLD) {
       const T g1 = R[RO] * v2;
-      aR1 = ((g1 + B2) + sqrt(fmax2((g1 + B2) * (g1 + B2) - g1 * f2, T(0)))) / (2 * R[RO]);
+      aR1 = div_<T, FAST>((g1 + B2) + sqrt(fmax2((g1 + B2) * (g1 + B2) - g1 * f2, T(0))), 2 * R[RO]);
     }
   }
 
@@ -150,7 +195,7 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
     f1 = sqrt(fmax2(aL, aR));
     aL = fmin2(fmin2(L[vn], R[vn]) - f1, T(0));
     aR = fmax2(fmax2(L[vn], R[vn]) + f1, T(0));
-    f1 = T(1) / (aR - aL);
+    f1 = rcp_<T, FAST>(aR - aL);
     f2 = aL * aR;
 #pragma unroll
     for (int v = MX; v <= EN; ++v) Fo[v] = f1 * (aR * FL[v] - aL * FR[v] + f2 * (UR[v] - UL[v]));
@@ -162,7 +207,7 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
     f1 = sqrt(fmax2(aL, aR));
     aL = fmin2(fmin2(L[vn], R[vn]) - f1, T(0));
     aR = fmax2(fmax2(L[vn], R[vn]) + f1, T(0));
-    f1 = T(1) / (aR - aL);
+    f1 = rcp_<T, FAST>(aR - aL);
     f2 = aL * aR;
 #pragma unroll
     for (int v = MX; v <= MZ; ++v) Uh[v] = f1 * (aR * UR[v] - aL * UL[v] - FR[v] + FL[v]);
@@ -170,19 +215,17 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
     for (int v = RO; v <= BZ; ++v) Uh[v] = f1 * (aR * R[v] - aL * L[v] - FR[v] + FL[v]);
     Fo[bt1] = f1 * (aR * FL[bt1] - aL * FR[bt1] + f2 * (R[bt1] - L[bt1]));
     Fo[bt2] = f1 * (aR * FL[bt2] - aL * FR[bt2] + f2 * (R[bt2] - L[bt2]));
-    f2 = T(1) / Uh[RO];
+    f2 = rcp_<T, FAST>(Uh[RO]);
     const T aM = Uh[mn] * f2;
     const T at1 = Uh[mt1] * f2;
     const T at2 = Uh[mt2] * f2;
     const T pt = ptL + L[RO] * (aL - L[vn]) * (aM - L[vn]);
-    const T roL = L[RO] * (aL - L[vn]) / (aL - aM);
-    const T enL = ((aL - L[vn]) * UL[EN] - ptL * L[vn] + pt * aM +
-                   Uh[bn] * (vBL - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])) /
-                  (aL - aM);
-    const T roR = R[RO] * (aR - R[vn]) / (aR - aM);
-    const T enR = ((aR - R[vn]) * UR[EN] - ptR * R[vn] + pt * aM +
-                   Uh[bn] * (vBR - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])) /
-                  (aR - aM);
+    const T roL = div_<T, FAST>(L[RO] * (aL - L[vn]), aL - aM);
+    const T enL = div_<T, FAST>(((aL - L[vn]) * UL[EN] - ptL * L[vn] + pt * aM +
+                   Uh[bn] * (vBL - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])), (aL - aM));
+    const T roR = div_<T, FAST>(R[RO] * (aR - R[vn]), aR - aM);
+    const T enR = div_<T, FAST>(((aR - R[vn]) * UR[EN] - ptR * R[vn] + pt * aM +
+                   Uh[bn] * (vBR - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])), (aR - aM));
     f1 = T(0.5) + fsign(T(0.5), aM);
     f2 = T(1) - f1;
     Fo[mn] = f1 * (aL * (roL * aM - UL[mn]) + FL[mn]) + f2 * (aR * (roR * aM - UR[mn]) + FR[mn]);
@@ -193,7 +236,7 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   } else {  // HLLD :408-576 / LHLLD :648-780
     T psi = T(0);
     if (TYPE == FX_LHLLD) {
-      f1 = fmin2(T(1), fmax2(aL1, aR1) / fmax2(aL, aR));
+      f1 = fmin2(T(1), div_<T, FAST>(fmax2(aL1, aR1), fmax2(aL, aR)));
       psi = 2 * sqrt(f1) - f1;
     }
     f1 = sqrt(fmax2(aL, aR));
@@ -207,37 +250,41 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
       for (int v = 0; v < NV; ++v) Fo[v] = FR[v];
     } else {
       T Uh[NV];
-      f1 = T(1) / (aR - aL);
+      f1 = rcp_<T, FAST>(aR - aL);
 #pragma unroll
       for (int v = MX; v <= MZ; ++v) Uh[v] = f1 * (aR * UR[v] - aL * UL[v] - FR[v] + FL[v]);
 #pragma unroll
       for (int v = RO; v <= BZ; ++v) Uh[v] = f1 * (aR * R[v] - aL * L[v] - FR[v] + FL[v]);
-      const T aM = Uh[mn] / Uh[RO];
+      const T aM = div_<T, FAST>(Uh[mn], Uh[RO]);
       T pt;
       if (TYPE == FX_LHLLD) {
-        pt = (R[RO] * ptL * (aR - R[vn]) - L[RO] * ptR * (aL - L[vn]) +
-              psi * L[RO] * R[RO] * (aR - R[vn]) * (aL - L[vn]) * (R[vn] - L[vn])) /
-             (R[RO] * (aR - R[vn]) - L[RO] * (aL - L[vn]));
+        pt = div_<T, FAST>(R[RO] * ptL * (aR - R[vn]) - L[RO] * ptR * (aL - L[vn]) +
+                               psi * L[RO] * R[RO] * (aR - R[vn]) * (aL - L[vn]) * (R[vn] - L[vn]),
+                           R[RO] * (aR - R[vn]) - L[RO] * (aL - L[vn]));
       } else {
         pt = ptL + L[RO] * (aL - L[vn]) * (aM - L[vn]);
       }
-      const T roL = L[RO] * (aL - L[vn]) / (aL - aM);
-      const T roR = R[RO] * (aR - R[vn]) / (aR - aM);
-      const T aVL = fabs(Uh[bn]) / sqrt(roL);
-      const T aVR = fabs(Uh[bn]) / sqrt(roR);
+      const T roL = div_<T, FAST>(L[RO] * (aL - L[vn]), aL - aM);
+      const T roR = div_<T, FAST>(R[RO] * (aR - R[vn]), aR - aM);
+      // Alfven speeds; the FAST variant keeps 1/sqrt(rho*) for the central states
+      T rsL = T(0), rsR = T(0);
+      if constexpr (FAST && sizeof(T) == 8) {
+        rsL = rsqrt_nr(roL);
+        rsR = rsqrt_nr(roR);
+      }
+      const T aVL = (FAST && sizeof(T) == 8) ? fabs(Uh[bn]) * rsL : fabs(Uh[bn]) / sqrt(roL);
+      const T aVR = (FAST && sizeof(T) == 8) ? fabs(Uh[bn]) * rsR : fabs(Uh[bn]) / sqrt(roR);
       if (TYPE == FX_HLLD && ((aL >= (aM - hllg_factor * aVL)) || ((aM + hllg_factor * aVR) >= aR))) {
         // HLLC-G fallback :450-476
         f2 = aL * aR;
         Fo[bt1] = f1 * (aR * FL[bt1] - aL * FR[bt1] + f2 * (R[bt1] - L[bt1]));
         Fo[bt2] = f1 * (aR * FL[bt2] - aL * FR[bt2] + f2 * (R[bt2] - L[bt2]));
-        const T at1 = Uh[mt1] / Uh[RO];
-        const T at2 = Uh[mt2] / Uh[RO];
-        const T enL = ((aL - L[vn]) * UL[EN] - ptL * L[vn] + pt * aM +
-                       Uh[bn] * (vBL - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])) /
-                      (aL - aM);
-        const T enR = ((aR - R[vn]) * UR[EN] - ptR * R[vn] + pt * aM +
-                       Uh[bn] * (vBR - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])) /
-                      (aR - aM);
+        const T at1 = div_<T, FAST>(Uh[mt1], Uh[RO]);
+        const T at2 = div_<T, FAST>(Uh[mt2], Uh[RO]);
+        const T enL = div_<T, FAST>(((aL - L[vn]) * UL[EN] - ptL * L[vn] + pt * aM +
+                       Uh[bn] * (vBL - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])), (aL - aM));
+        const T enR = div_<T, FAST>(((aR - R[vn]) * UR[EN] - ptR * R[vn] + pt * aM +
+                       Uh[bn] * (vBR - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])), (aR - aM));
         f1 = T(0.5) + fsign(T(0.5), aM);
         f2 = T(1) - f1;
         Fo[mn] = f1 * (aL * (roL * aM - UL[mn]) + FL[mn]) + f2 * (aR * (roR * aM - UR[mn]) + FR[mn]);
@@ -249,29 +296,27 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
         T UL1[NV], UR1[NV];
         // L* (:482-493)
         const T tL = aL - L[vn];
-        f1 = T(1) / (L[RO] * tL * (aL - aM) - Uh[bn] * Uh[bn]);
+        f1 = rcp_<T, FAST>(L[RO] * tL * (aL - aM) - Uh[bn] * Uh[bn]);
         UL1[bt1] = L[bt1] * f1 * (L[RO] * (tL * tL) - Uh[bn] * Uh[bn]);
         UL1[bt2] = L[bt2] * f1 * (L[RO] * (tL * tL) - Uh[bn] * Uh[bn]);
         const T vt1L = L[vt1] - f1 * Uh[bn] * L[bt1] * (aM - L[vn]);
         const T vt2L = L[vt2] - f1 * Uh[bn] * L[bt2] * (aM - L[vn]);
         UL1[RO] = roL;
-        UL1[EN] = ((aL - L[vn]) * UL[EN] - ptL * L[vn] + pt * aM +
-                   Uh[bn] * (vBL - aM * Uh[bn] - vt1L * UL1[bt1] - vt2L * UL1[bt2])) /
-                  (aL - aM);
+        UL1[EN] = div_<T, FAST>(((aL - L[vn]) * UL[EN] - ptL * L[vn] + pt * aM +
+                   Uh[bn] * (vBL - aM * Uh[bn] - vt1L * UL1[bt1] - vt2L * UL1[bt2])), (aL - aM));
         UL1[mn] = roL * aM;
         UL1[mt1] = roL * vt1L;
         UL1[mt2] = roL * vt2L;
         // R* (:496-507)
         const T tR = aR - R[vn];
-        f1 = T(1) / (R[RO] * tR * (aR - aM) - Uh[bn] * Uh[bn]);
+        f1 = rcp_<T, FAST>(R[RO] * tR * (aR - aM) - Uh[bn] * Uh[bn]);
         UR1[bt1] = R[bt1] * f1 * (R[RO] * (tR * tR) - Uh[bn] * Uh[bn]);
         UR1[bt2] = R[bt2] * f1 * (R[RO] * (tR * tR) - Uh[bn] * Uh[bn]);
         const T vt1R = R[vt1] - f1 * Uh[bn] * R[bt1] * (aM - R[vn]);
         const T vt2R = R[vt2] - f1 * Uh[bn] * R[bt2] * (aM - R[vn]);
         UR1[RO] = roR;
-        UR1[EN] = ((aR - R[vn]) * UR[EN] - ptR * R[vn] + pt * aM +
-                   Uh[bn] * (vBR - aM * Uh[bn] - vt1R * UR1[bt1] - vt2R * UR1[bt2])) /
-                  (aR - aM);
+        UR1[EN] = div_<T, FAST>(((aR - R[vn]) * UR[EN] - ptR * R[vn] + pt * aM +
+                   Uh[bn] * (vBR - aM * Uh[bn] - vt1R * UR1[bt1] - vt2R * UR1[bt2])), (aR - aM));
         UR1[mn] = roR * aM;
         UR1[mt1] = roR * vt1R;
         UR1[mt2] = roR * vt2R;
@@ -291,9 +336,9 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
           Fo[bt2] = aR * (UR1[bt2] - R[bt2]) + FR[bt2];
         } else {  // central states :533-572
           T U2[NV];
-          const T roLs = sqrt(roL);
-          const T roRs = sqrt(roR);
-          f1 = T(1) / (roLs + roRs);
+          const T roLs = (FAST && sizeof(T) == 8) ? roL * rsL : sqrt(roL);
+          const T roRs = (FAST && sizeof(T) == 8) ? roR * rsR : sqrt(roR);
+          f1 = rcp_<T, FAST>(roLs + roRs);
           f2 = fsign(T(1), Uh[bn]);
           const T at1 = f1 * (roLs * vt1L + roRs * vt1R + (UR1[bt1] - UL1[bt1]) * f2);
           const T at2 = f1 * (roLs * vt2L + roRs * vt2R + (UR1[bt2] - UL1[bt2]) * f2);
@@ -332,10 +377,10 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
 }
 
 // Fast magnetosonic speed used by set_dt (2D_basic/set_dt.f90:27-34).
-template <class T>
+template <class T, bool FAST = false>
 __device__ __forceinline__ T fast_speed(T f1, T B2, T bd, T ro) {
   const T f2 = 4 * f1 * (bd * bd);
-  return sqrt(((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f2, T(0)))) / (2 * ro));
+  return sqrt(div_<T, FAST>((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f2, T(0))), 2 * ro));
 }
 
 }  // namespace omhd

@@ -15,6 +15,7 @@ from dataclasses import dataclass, field
 
 from . import _lib
 
+OMHD_TIMEOUT = 5  # omhd_status_t
 LIMITERS = {"flat": 0, "minmod": 1, "mc": 2, "vanleer": 3, "koren": 4}
 FLUXES = {"llf": 0, "hll": 1, "hllc": 2, "hlld": 3, "lhlld": 4}
 PRECISIONS = {"fp64": 0, "fp64_parity": 1, "mixed": 2}
@@ -266,11 +267,15 @@ class Solver:
         in batches; kernels turn themselves off once t >= tend, so the step
         count matches the reference's loop exactly."""
         self.set_tend(tend)
+        last = -1
         while True:
             self.step(batch)
-            info = self.sync()
+            info = self.sync()  # raises on a device-reported failure
             if info.done:
                 return info
+            if info.steps == last:
+                raise OmhdError(OMHD_TIMEOUT, "run_until made no progress")
+            last = info.steps
 
     @property
     def launches_per_step(self) -> int:

@@ -189,7 +189,7 @@ class Grid:
         self.last_ch = ch.value
         return self
 
-    def run_until(self, tend: float, max_steps: int = 10**9):
+    def run_until(self, tend: float, max_steps: int = 100000):
         while self.t < tend and self.steps < max_steps:  # main.f90:73
             self.step(1)
         return self

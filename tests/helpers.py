@@ -28,13 +28,7 @@ def random_state(shape_xyz, seed: int = 0, smooth: bool = False) -> np.ndarray:
     return np.ascontiguousarray(U)
 
 
-def rel_l1(a: np.ndarray, b: np.ndarray) -> np.ndarray:
-    """Per-variable relative L1 error of a against b over the leading axis."""
-    a = a.reshape(a.shape[0], -1)
-    b = b.reshape(b.shape[0], -1)
-    num = np.abs(a - b).sum(axis=1)
-    den = np.abs(b).sum(axis=1)
-    return np.where(den > 0, num / np.where(den > 0, den, 1.0), num)
+from openmhd_gb300.metrics import rel_l1, scaled_l1  # noqa: E402,F401
 
 
 def interior(U: np.ndarray) -> np.ndarray:
