@@ -264,6 +264,26 @@ int omhd_solver_last_error(omhd_solver* s, omhd_error_info* info);
 /* kernels launched by the last omhd_solver_step call per step (for accounting) */
 int omhd_solver_launches_per_step(omhd_solver* s);
 
+/* ======================================================================
+ * Fused 2D step without any device allocation (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc -- drivers inside an
+ * application whose framework owns the whole device memory pool, or jobs
+ * that must reserve all device memory when the program loads.  The stage
+ * buffer, step record, error word and coordinates live in one static device
+ * array of omhd_step2d_noalloc_max_doubles() doubles (32 MiB) that every GPU
+ * loading the library holds until exit; grids needing more scratch than that
+ * (9*ix*jx + ix + jx + 64 doubles, about 419k cells) are rejected with
+ * OMHD_BAD_ARG and a message in omhd_last_error().  U must be device memory
+ * (ix*jx*9 doubles, reference layout); bc is applied to it, then nsteps
+ * steps run from time t0 on `stream` and the call waits for them.  Every call
+ * reuses the same array: calls that overlap on the GPU race.  The first call
+ * on a device (with it current) looks up the array's device address, so it
+ * should come before any stream capture.
+ * ==================================================================== */
+int omhd_step2d_noalloc(double* U_dev, const omhd_config* cfg, double t0, int nsteps, void* stream,
+                        omhd_step_info* info);
+size_t omhd_step2d_noalloc_max_doubles(void);
+
 #ifdef __cplusplus
 }
 #endif

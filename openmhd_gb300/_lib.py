@@ -109,6 +109,8 @@ SIGNATURES = [
     ("omhd_solver_sync", I, [P, C.POINTER(StepInfo)]),
     ("omhd_solver_last_error", I, [P, C.POINTER(ErrorInfo)]),
     ("omhd_solver_launches_per_step", I, [P]),
+    ("omhd_step2d_noalloc", I, [P, C.POINTER(Config), D, I, P, C.POINTER(StepInfo)]),
+    ("omhd_step2d_noalloc_max_doubles", C.c_size_t, []),
 ]
 
 

@@ -32,6 +32,7 @@ UNITS = {
     "omhd_fused3d_fp64.cu": ["--fmad=true"],
     "omhd_fused3d_parity.cu": ["--fmad=false"],
     "omhd_fused3d_mixed.cu": ["--fmad=true"],
+    "omhd_noalloc.cu": [],
 }
 
 

@@ -12,7 +12,7 @@ HEADER = os.path.join(ROOT, "include", "openmhd_gb300.h")
 def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    names = re.findall(r"^\s*(?:int|void|double)\s+\**\s*(\w+)\s*\(", text, flags=re.M)
+    names = re.findall(r"^\s*(?:int|void|double|size_t)\s+\**\s*(\w+)\s*\(", text, flags=re.M)
     return sorted(set(names))
 
 
