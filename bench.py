@@ -327,6 +327,33 @@ def _fp64_peak_gflops(lib) -> float:
     return g.value
 
 
+def run_profile(args):
+    """Small fixed run for profiler captures: --nx x --ny KH grid, one
+    precision, warm-up + steps stage launches and nothing else."""
+    import torch
+
+    from openmhd_gb300 import Solver, harris3d, kelvin_helmholtz
+
+    if args.nz:
+        cfg, model = harris3d(args.nx, args.ny, args.nz, precision=args.precision)
+    else:
+        cfg, model = kelvin_helmholtz(args.nx, args.ny, precision=args.precision)
+    s = Solver(cfg).init_model(model)
+    s.step(args.warmup)
+    s.sync()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s.stream)
+    s.step(args.steps)
+    e1.record(s.stream)
+    info = s.sync()
+    ms = e0.elapsed_time(e1) / max(args.steps, 1)
+    print(json.dumps({"profile": True, "nx": args.nx, "ny": args.ny, "nz": args.nz, "precision": args.precision,
+                      "ms_per_step": ms, "cell_updates_per_s": cfg.interior_cells / (ms / 1e3),
+                      "status": info.status, "steps": info.steps}), flush=True)
+    return 0 if info.status == 0 else 1
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -334,7 +361,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="small fixed run for profiler captures")
+    ap.add_argument("--nx", type=int, default=NX)
+    ap.add_argument("--ny", type=int, default=NY)
+    ap.add_argument("--nz", type=int, default=0)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_parity", "mixed"])
     args = ap.parse_args()
+    if args.profile:
+        from openmhd_gb300.build import build
+
+        build()
+        return run_profile(args)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
