@@ -265,6 +265,30 @@ int omhd_solver_last_error(omhd_solver* s, omhd_error_info* info);
 int omhd_solver_launches_per_step(omhd_solver* s);
 
 /* ======================================================================
+ * Ensembles of independent 2D problems (no counterpart in the reference,
+ * which runs one problem per program): every member keeps its own grid size,
+ * boundaries, model and dt; all members advance together with one persistent
+ * batched kernel per RK stage.  Members must share nd = 2, the flux type
+ * (HLLD) and the precision (OMHD_PREC_MIXED or OMHD_PREC_FP64).
+ * ==================================================================== */
+typedef struct omhd_ensemble omhd_ensemble;
+int omhd_ensemble_create(const omhd_config* cfgs, int n, omhd_ensemble** out);
+int omhd_ensemble_destroy(omhd_ensemble* e);
+int omhd_ensemble_size(omhd_ensemble* e);
+int omhd_ensemble_set_stream(omhd_ensemble* e, void* cuda_stream);
+/* member i as a solver handle (state pointer, put/get state, coordinates) */
+int omhd_ensemble_member(omhd_ensemble* e, int i, omhd_solver** s);
+int omhd_ensemble_init_models(omhd_ensemble* e, const omhd_model* models);
+/* tile_kind 0: 32x8, 1: 32x4, 2: 16x16, 3: 64x4 cells per CTA; CTAs = ctas_per_sm x SMs */
+int omhd_ensemble_set_tiling(omhd_ensemble* e, int tile_kind, int ctas_per_sm);
+/* time `steps` real steps per candidate tiling and keep the fastest */
+int omhd_ensemble_autotune(omhd_ensemble* e, int steps, int* tile_kind, int* ctas_per_sm, double* ms_per_step);
+int omhd_ensemble_step(omhd_ensemble* e, int nsteps);
+int omhd_ensemble_step_graph(omhd_ensemble* e, int nsteps, int replays);
+/* waits; infos (n entries, may be NULL) get every member's step record */
+int omhd_ensemble_sync(omhd_ensemble* e, omhd_step_info* infos);
+
+/* ======================================================================
  * Fused 2D step without any device allocation (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc -- drivers inside an
  * application whose framework owns the whole device memory pool, or jobs

@@ -109,6 +109,17 @@ SIGNATURES = [
     ("omhd_solver_sync", I, [P, C.POINTER(StepInfo)]),
     ("omhd_solver_last_error", I, [P, C.POINTER(ErrorInfo)]),
     ("omhd_solver_launches_per_step", I, [P]),
+    ("omhd_ensemble_create", I, [C.POINTER(Config), I, C.POINTER(C.c_void_p)]),
+    ("omhd_ensemble_destroy", I, [P]),
+    ("omhd_ensemble_size", I, [P]),
+    ("omhd_ensemble_set_stream", I, [P, P]),
+    ("omhd_ensemble_member", I, [P, I, C.POINTER(C.c_void_p)]),
+    ("omhd_ensemble_init_models", I, [P, C.POINTER(Model)]),
+    ("omhd_ensemble_set_tiling", I, [P, I, I]),
+    ("omhd_ensemble_autotune", I, [P, I, c_int_p, c_int_p, c_double_p]),
+    ("omhd_ensemble_step", I, [P, I]),
+    ("omhd_ensemble_step_graph", I, [P, I, I]),
+    ("omhd_ensemble_sync", I, [P, C.POINTER(StepInfo)]),
     ("omhd_step2d_noalloc", I, [P, C.POINTER(Config), D, I, P, C.POINTER(StepInfo)]),
     ("omhd_step2d_noalloc_max_doubles", C.c_size_t, []),
 ]

@@ -33,6 +33,7 @@ UNITS = {
     "omhd_fused3d_parity.cu": ["--fmad=false"],
     "omhd_fused3d_mixed.cu": ["--fmad=true"],
     "omhd_noalloc.cu": [],
+    "omhd_ensemble.cu": [],
 }
 
 

@@ -34,6 +34,17 @@ struct StageArgs {
 int launch_stage2d_fp64(const StageArgs& a, cudaStream_t s);
 int launch_stage2d_parity(const StageArgs& a, cudaStream_t s);
 int launch_stage2d_mixed(const StageArgs& a, cudaStream_t s);
+// ensemble launchers: tile_kind 0: 32x8, 1: 32x4, 2: 16x16, 3: 64x4 cells per CTA
+int launch_batch2d_fp64(int flux, int tile_kind, const StageArgs* args_dev, const int* tile_start_dev, int ngrids,
+                        int total_tiles, int ctas, cudaStream_t s);
+int launch_batch2d_mixed(int flux, int tile_kind, const StageArgs* args_dev, const int* tile_start_dev, int ngrids,
+                         int total_tiles, int ctas, cudaStream_t s);
+constexpr int kBatchTileKinds = 4;
+inline void batch_tile_dims(int kind, int* tx, int* ty) {
+  static const int d[4][2] = {{32, 8}, {32, 4}, {16, 16}, {64, 4}};
+  *tx = d[kind & 3][0];
+  *ty = d[kind & 3][1];
+}
 int launch_stage3d_fp64(const StageArgs& a, cudaStream_t s);
 int launch_stage3d_parity(const StageArgs& a, cudaStream_t s);
 int launch_stage3d_mixed(const StageArgs& a, cudaStream_t s);

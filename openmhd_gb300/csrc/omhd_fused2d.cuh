@@ -4,16 +4,19 @@
 // two-cell halo of the state in shared memory.  Inside the CTA:
 //   A  load + conserved->primitive recovery (u2v.f90) of the halo tile,
 //      stage 1 applies the first GLM half (glm_ss2.f90) on the fly;
-//   B  x-direction slope limiting (limiter.f90) -> face states, wall fix;
-//   C  x-face Riemann fluxes (flux_solver.f90) [+ resistive terms];
-//   D  x flux differences kept in registers (FP64);
-//   E/F the same in y;
-//   G  Runge-Kutta update (rk.f90), ghost-cell fill by the owner of each
-//      source cell (bc.f90), stage 2 applies the second GLM half and reduces
-//      the next step's CFL speed (set_dt.f90); the last CTA plans the next
-//      step on the device.
+//   B  slope limiting (limiter.f90) in x and y -> face states of both
+//      directions in one phase, then the wall face fixes (bc_for_F/G);
+//   C  Riemann fluxes (flux_solver.f90) [+ resistive terms] of all x faces
+//      and all y faces of the tile in one phase, warp-aligned so that no warp
+//      mixes directions;
+//   D  Runge-Kutta update (rk.f90) from the flux differences (FP64),
+//      ghost-cell fill by the owner of each source cell (bc.f90); stage 2
+//      applies the second GLM half and reduces the next step's CFL speed
+//      (set_dt.f90); the last CTA plans the next step on the device.
 // Per stage this reads the state once (plus halo) and writes it once: the
 // face states and fluxes of the reference (VL, VR, F, G) never reach HBM.
+// Three CTA-wide barriers per stage; the FP64 pipe is the bottleneck on
+// GB300, so phases are arranged to keep every warp issuing FP64 work.
 //
 // Included by one translation unit per arithmetic variant; OMHD_VARIANT names
 // the namespace so that instantiations built with different floating-point
@@ -29,15 +32,27 @@
 namespace omhd {
 namespace OMHD_VARIANT {
 
-constexpr int TX = 32, TY = 8, NT = TX * TY;
-constexpr int RX = TX + 4, RY = TY + 4;
-constexpr int SFACE = (TY * (TX + 2) > (TY + 2) * TX) ? TY * (TX + 2) : (TY + 2) * TX;
-constexpr int SFLUX = (TY * (TX + 1) > (TY + 1) * TX) ? TY * (TX + 1) : (TY + 1) * TX;
+constexpr int round32(int n) { return (n + 31) / 32 * 32; }
+constexpr int imax(int a, int b) { return a > b ? a : b; }
 
-template <class T>
-constexpr size_t smem2d_bytes() {
-  return sizeof(T) * (size_t)NV * (RY * RX + 2 * SFACE + SFLUX);
-}
+// tile geometry: TX x TY interior cells
+template <int TX_, int TY_>
+struct Geo2 {
+  static constexpr int TX = TX_, TY = TY_;
+  static constexpr int RX = TX + 4, RY = TY + 4;  // halo tile
+  static constexpr int NXS = TY * (TX + 2);       // cells reconstructed in x
+  static constexpr int NYS = (TY + 2) * TX;       // cells reconstructed in y
+  static constexpr int NXF = TY * (TX + 1);       // x faces
+  static constexpr int NYF = (TY + 1) * TX;       // y faces
+  static constexpr int NXFP = round32(NXF);       // x faces padded to whole warps
+  // one thread per y face (or padded x face), at least one per cell
+  static constexpr int NT = imax(imax(NXFP, round32(NYF)), round32(TX * TY));
+  template <class T>
+  static constexpr size_t smem_bytes() {
+    return sizeof(T) * (size_t)NV * (RY * RX + 2 * (NXS + NYS) + NXF + NYF);
+  }
+};
+using GeoDefault = Geo2<32, 8>;
 
 __device__ __forceinline__ int map_index(int g, int n, bool periodic) {
   if (g >= 0 && g < n) return g;
@@ -62,22 +77,27 @@ __device__ __forceinline__ double eta_at(int kind, double x, double y, double z)
   return 0.0;
 }
 
-template <class T, int FLUX>
-__global__ void __launch_bounds__(NT) k_stage2d(const StageArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+// One stage on one tile (tile coordinates bxi, byi) of the grid described by
+// `a`; returns this thread's CFL speed of the updated cell (stage 2) or 0.
+// All threads of the CTA must call it (it synchronises the CTA).
+template <class T, int FLUX, class G>
+__device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int byi, unsigned char* smem_raw,
+                                               double dt, double chd, double glmf) {
+  constexpr int TX = G::TX, TY = G::TY, NT = G::NT, RX = G::RX, RY = G::RY;
+  constexpr int NXS = G::NXS, NYS = G::NYS, NXF = G::NXF, NYF = G::NYF, NXFP = G::NXFP;
+  constexpr int PL = RX * RY;
   T* W = reinterpret_cast<T*>(smem_raw);  // [NV][RY][RX] primitive halo tile
-  T* SL = W + NV * RY * RX;               // [NV][SFACE] upper-face states of cells
-  T* SR = SL + NV * SFACE;                // [NV][SFACE] lower-face states of cells
-  T* FB = SR + NV * SFACE;                // [NV][SFLUX] face fluxes
-  __shared__ double red32[32];
+  T* SLx = W + NV * PL;                   // [NV][NXS] upper x-face states of cells
+  T* SRx = SLx + NV * NXS;                // [NV][NXS] lower x-face states of cells
+  T* SLy = SRx + NV * NXS;                // [NV][NYS]
+  T* SRy = SLy + NV * NYS;                // [NV][NYS]
+  T* FBx = SRy + NV * NYS;                // [NV][NXF] x-face fluxes
+  T* FBy = FBx + NV * NXF;                // [NV][NYF] y-face fluxes
 
-  StepState* st = a.st;
-  if (st->done || *(volatile int*)&a.err->code) return;
-  const double dt = st->dt, chd = st->ch, glmf = st->glm_f;
   const int ix = a.ix, jx = a.jx;
   const size_t N = (size_t)ix * jx;
   const int tid = threadIdx.x;
-  const int gi0 = 1 + blockIdx.x * TX, gj0 = 1 + blockIdx.y * TY;
+  const int gi0 = 1 + bxi * TX, gj0 = 1 + byi * TY;
   const bool perx = a.bc_kind[0] == OMHD_BC_PERIODIC, pery = a.bc_kind[2] == OMHD_BC_PERIODIC;
   const bool resist = a.eta_kind != OMHD_ETA_NONE;
   const double gamma = a.gamma;
@@ -87,7 +107,7 @@ __global__ void __launch_bounds__(NT) k_stage2d(const StageArgs a) {
   const int lm = a.lm_type;
 
   // ---- A: halo tile load + u2v (+ first GLM half in stage 1) ----
-  for (int q = tid; q < RX * RY; q += NT) {
+  for (int q = tid; q < PL; q += NT) {
     const int rx = q % RX, ry = q / RX;
     const bool cx_in = rx >= 2 && rx < TX + 2, cy_in = ry >= 2 && ry < TY + 2;
     if (!cx_in && !cy_in) {
@@ -107,16 +127,15 @@ __global__ void __launch_bounds__(NT) k_stage2d(const StageArgs a) {
     const double pr = f1g * (U[EN * N + c] - 0.5 * (rv2 + B2));  // u2v.f90:27
     double ps = U[PS * N + c];
     if (a.stage == 1) ps = glmf * ps;
-    const int o = ry * RX + rx;
-    W[VX * RY * RX + o] = T(vx);
-    W[VY * RY * RX + o] = T(vy);
-    W[VZ * RY * RX + o] = T(vz);
-    W[PR * RY * RX + o] = T(pr);
-    W[RO * RY * RX + o] = T(ro);
-    W[BX * RY * RX + o] = T(bx);
-    W[BY * RY * RX + o] = T(by);
-    W[BZ * RY * RX + o] = T(bz);
-    W[PS * RY * RX + o] = T(ps);
+    W[VX * PL + q] = T(vx);
+    W[VY * PL + q] = T(vy);
+    W[VZ * PL + q] = T(vz);
+    W[PR * PL + q] = T(pr);
+    W[RO * PL + q] = T(ro);
+    W[BX * PL + q] = T(bx);
+    W[BY * PL + q] = T(by);
+    W[BZ * PL + q] = T(bz);
+    W[PS * PL + q] = T(ps);
     if (cx_in && cy_in && gi <= ix - 2 && gj <= jx - 2) {  // owner check, u2v.f90:36-45
       if (pr <= 0)
         raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, 0, 0, pr);
@@ -126,187 +145,207 @@ __global__ void __launch_bounds__(NT) k_stage2d(const StageArgs a) {
   }
   __syncthreads();
 
-  // ---- B: x slopes for cells rx = 1 .. TX+2 on tile rows ----
-  constexpr int XS = TX + 2;  // face-state row length in the x pass
-  for (int q = tid; q < TY * XS; q += NT) {
-    const int cx = q % XS, cy = q / XS;
-    const int o = (cy + 2) * RX + (cx + 1);
+  // ---- B: slopes in x (cells rx = 1..TX+2 on tile rows) and y (rows
+  //      ry = 1..TY+2 on tile columns) ----
+  constexpr int XS = TX + 2;
+  for (int q = tid; q < NXS + NYS; q += NT) {
+    int o, st;
+    T *dl, *dr;
+    int qq;
+    if (q < NXS) {
+      const int cx = q % XS, cy = q / XS;
+      o = (cy + 2) * RX + (cx + 1);
+      st = 1;
+      dl = SLx;
+      dr = SRx;
+      qq = q;
+    } else {
+      qq = q - NXS;
+      const int cx = qq % TX, cy = qq / TX;
+      o = (cy + 1) * RX + (cx + 2);
+      st = RX;
+      dl = SLy;
+      dr = SRy;
+    }
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       T l, r;
-      reconstruct<T>(lm, W[v * RY * RX + o - 1], W[v * RY * RX + o], W[v * RY * RX + o + 1], l, r);
-      SL[v * SFACE + q] = l;
-      SR[v * SFACE + q] = r;
+      reconstruct_t<T, OMHD_FAST>(lm, W[v * PL + o - st], W[v * PL + o], W[v * PL + o + st], l, r);
+      dl[v * (q < NXS ? NXS : NYS) + qq] = l;
+      dr[v * (q < NXS ? NXS : NYS) + qq] = r;
     }
   }
   __syncthreads();
-  // wall face fix (2D_KH/bc.f90:42-51 pattern; 2D_reconnection/bc.f90:136-165)
-  if (!perx) {
-    if (gi0 == 1 && tid < TY * NV) {  // west face: VL = flip(VR)
+  // wall face fixes: x walls (2D_reconnection/bc.f90:136-165), y walls (2D_KH/bc.f90:55-83)
+  if (!perx || !pery) {
+    if (!perx && tid < TY * NV) {
       const int cy = tid % TY, v = tid / TY;
-      const T s = SR[v * SFACE + cy * XS + 1];
-      SL[v * SFACE + cy * XS + 0] = ((a.bc_flip[0] >> v) & 1) ? -s : s;
+      if (gi0 == 1) {  // west face: VL = flip(VR)
+        const T s = SRx[v * NXS + cy * XS + 1];
+        SLx[v * NXS + cy * XS + 0] = ((a.bc_flip[0] >> v) & 1) ? -s : s;
+      }
+      const int cl = (ix - 2) - gi0 + 1;  // cx of the last interior cell
+      if (cl >= 1 && cl <= TX) {          // east face: VR = flip(VL)
+        const T s = SLx[v * NXS + cy * XS + cl];
+        SRx[v * NXS + cy * XS + cl + 1] = ((a.bc_flip[1] >> v) & 1) ? -s : s;
+      }
     }
-    const int cl = (ix - 2) - gi0 + 1;  // cx of the last interior cell
-    if (cl >= 1 && cl <= TX && tid < TY * NV) {  // east face: VR = flip(VL)
-      const int cy = tid % TY, v = tid / TY;
-      const T s = SL[v * SFACE + cy * XS + cl];
-      SR[v * SFACE + cy * XS + cl + 1] = ((a.bc_flip[1] >> v) & 1) ? -s : s;
+    if (!pery && tid >= NT - TX) {
+      const int cx = tid - (NT - TX);
+      const int cl = (jx - 2) - gj0 + 1;
+      for (int v = 0; v < NV; ++v) {
+        if (gj0 == 1) {  // south face: VL = flip(VR)
+          const T s = SRy[v * NYS + 1 * TX + cx];
+          SLy[v * NYS + 0 * TX + cx] = ((a.bc_flip[2] >> v) & 1) ? -s : s;
+        }
+        if (cl >= 1 && cl <= TY) {  // north face: VR = flip(VL)
+          const T s = SLy[v * NYS + cl * TX + cx];
+          SRy[v * NYS + (cl + 1) * TX + cx] = ((a.bc_flip[3] >> v) & 1) ? -s : s;
+        }
+      }
     }
     __syncthreads();
   }
 
-  // ---- C: x-face fluxes ----
+  // ---- C: fluxes of all x faces (work items 0..NXFP-1, padded to whole
+  //      warps) and all y faces (items NXFP..NXFP+NYF-1) ----
   constexpr int XF = TX + 1;
-  for (int q = tid; q < TY * XF; q += NT) {
-    const int fx = q % XF, cy = q / XF;
-    T L[NV], R[NV], Fo[NV];
+  for (int q = tid; q < NXFP + NYF; q += NT) {
+    if (q < NXFP) {
+      if (q >= NXF) continue;  // padding lanes
+      const int fx = q % XF, cy = q / XF;
+      T L[NV], R[NV], Fo[NV];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      L[v] = SL[v * SFACE + cy * XS + fx];
-      R[v] = SR[v * SFACE + cy * XS + fx + 1];
-    }
-    riemann_flux<T, 1, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
-    if (resist) {  // 2D_reconnection/flux_resistive.f90:266-283
-      const int g = gi0 - 1 + fx, gj = gj0 + cy;
-      if (g >= 0 && g <= ix - 2 && gj <= jx - 2) {
-        const int o = (cy + 2) * RX + (fx + 1);  // region index of cell g
-        auto B = [&](int var, int dxo, int dyo) { return double(W[var * RY * RX + o + dxo + dyo * RX]); };
-        const double odx = 1.0 / a.dx;
-        const double eta_dx = eta_at(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gj], 0.0) * odx;
-        const double JyS = -eta_dx * (B(BZ, 1, 0) - B(BZ, 0, 0));
-        const double JzS = eta_dx * ((B(BY, 1, 0) - B(BY, 0, 0)) -
-                                     0.25 * (B(BX, 0, 1) + B(BX, 1, 1) - B(BX, 0, -1) - B(BX, 1, -1)));
-        Fo[EN] = T(double(Fo[EN]) + 0.5 * (JyS * (B(BZ, 0, 0) + B(BZ, 1, 0)) - JzS * (B(BY, 0, 0) + B(BY, 1, 0))));
-        Fo[BY] = T(double(Fo[BY]) - JzS);
-        Fo[BZ] = T(double(Fo[BZ]) + JyS);
-      }
-    }
-#pragma unroll
-    for (int v = 0; v < NV; ++v) FB[v * SFLUX + q] = Fo[v];
-  }
-  __syncthreads();
-
-  // ---- D: x flux differences, F(i-1/2) - F(i+1/2), in FP64 ----
-  const int tx = tid % TX, ty = tid / TX;
-  double acc[NV];
-#pragma unroll
-  for (int v = 0; v < NV; ++v)
-    acc[v] = double(FB[v * SFLUX + ty * XF + tx]) - double(FB[v * SFLUX + ty * XF + tx + 1]);
-  __syncthreads();
-
-  // ---- E: y slopes for rows ry = 1 .. TY+2 on tile columns ----
-  for (int q = tid; q < (TY + 2) * TX; q += NT) {
-    const int cx = q % TX, cy = q / TX;
-    const int o = (cy + 1) * RX + (cx + 2);
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      T l, r;
-      reconstruct<T>(lm, W[v * RY * RX + o - RX], W[v * RY * RX + o], W[v * RY * RX + o + RX], l, r);
-      SL[v * SFACE + q] = l;
-      SR[v * SFACE + q] = r;
-    }
-  }
-  __syncthreads();
-  if (!pery) {
-    if (gj0 == 1 && tid < TX) {  // south face: VL = flip(VR)   (2D_KH/bc.f90:61-70)
       for (int v = 0; v < NV; ++v) {
-        const T s = SR[v * SFACE + 1 * TX + tid];
-        SL[v * SFACE + 0 * TX + tid] = ((a.bc_flip[2] >> v) & 1) ? -s : s;
+        L[v] = SLx[v * NXS + cy * XS + fx];
+        R[v] = SRx[v * NXS + cy * XS + fx + 1];
       }
-    }
-    const int cl = (jx - 2) - gj0 + 1;
-    if (cl >= 1 && cl <= TY && tid < TX) {  // north face: VR = flip(VL)  (2D_KH/bc.f90:72-81)
+      riemann_flux<T, 1, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
+      if (resist) {  // 2D_reconnection/flux_resistive.f90:266-283
+        const int g = gi0 - 1 + fx, gj = gj0 + cy;
+        if (g >= 0 && g <= ix - 2 && gj <= jx - 2) {
+          const int o = (cy + 2) * RX + (fx + 1);  // region index of cell g
+          auto B = [&](int var, int dxo, int dyo) { return double(W[var * PL + o + dxo + dyo * RX]); };
+          const double odx = 1.0 / a.dx;
+          const double eta_dx = eta_at(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gj], 0.0) * odx;
+          const double JyS = -eta_dx * (B(BZ, 1, 0) - B(BZ, 0, 0));
+          const double JzS = eta_dx * ((B(BY, 1, 0) - B(BY, 0, 0)) -
+                                       0.25 * (B(BX, 0, 1) + B(BX, 1, 1) - B(BX, 0, -1) - B(BX, 1, -1)));
+          Fo[EN] = T(double(Fo[EN]) + 0.5 * (JyS * (B(BZ, 0, 0) + B(BZ, 1, 0)) - JzS * (B(BY, 0, 0) + B(BY, 1, 0))));
+          Fo[BY] = T(double(Fo[BY]) - JzS);
+          Fo[BZ] = T(double(Fo[BZ]) + JyS);
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < NV; ++v) FBx[v * NXF + q] = Fo[v];
+    } else {
+      const int qq = q - NXFP;
+      const int cx = qq % TX, fy = qq / TX;
+      T L[NV], R[NV], Fo[NV];
+#pragma unroll
       for (int v = 0; v < NV; ++v) {
-        const T s = SL[v * SFACE + cl * TX + tid];
-        SR[v * SFACE + (cl + 1) * TX + tid] = ((a.bc_flip[3] >> v) & 1) ? -s : s;
+        L[v] = SLy[v * NYS + fy * TX + cx];
+        R[v] = SRy[v * NYS + (fy + 1) * TX + cx];
       }
-    }
-    __syncthreads();
-  }
-
-  // ---- F: y-face fluxes ----
-  for (int q = tid; q < (TY + 1) * TX; q += NT) {
-    const int cx = q % TX, fy = q / TX;
-    T L[NV], R[NV], Fo[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      L[v] = SL[v * SFACE + fy * TX + cx];
-      R[v] = SR[v * SFACE + (fy + 1) * TX + cx];
-    }
-    riemann_flux<T, 2, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
-    if (resist) {  // 2D_reconnection/flux_resistive.f90:289-306
-      const int gi = gi0 + cx, g = gj0 - 1 + fy;
-      if (g >= 0 && g <= jx - 2 && gi <= ix - 2) {
-        const int o = (fy + 1) * RX + (cx + 2);  // region index of cell (gi, g)
-        auto B = [&](int var, int dxo, int dyo) { return double(W[var * RY * RX + o + dxo + dyo * RX]); };
-        const double odx = 1.0 / a.dx;
-        const double eta_dx = eta_at(a.eta_kind, a.xc[gi], a.yc[g] + 0.5 * a.dx, 0.0) * odx;
-        const double JxS = eta_dx * (B(BZ, 0, 1) - B(BZ, 0, 0));
-        const double JzS = eta_dx * (0.25 * (B(BY, 1, 1) + B(BY, 1, 0) - B(BY, -1, 1) - B(BY, -1, 0)) -
-                                     (B(BX, 0, 1) - B(BX, 0, 0)));
-        Fo[EN] = T(double(Fo[EN]) + 0.5 * (JzS * (B(BX, 0, 0) + B(BX, 0, 1)) - JxS * (B(BZ, 0, 0) + B(BZ, 0, 1))));
-        Fo[BX] = T(double(Fo[BX]) + JzS);
-        Fo[BZ] = T(double(Fo[BZ]) - JxS);
+      riemann_flux<T, 2, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
+      if (resist) {  // 2D_reconnection/flux_resistive.f90:289-306
+        const int gi = gi0 + cx, g = gj0 - 1 + fy;
+        if (g >= 0 && g <= jx - 2 && gi <= ix - 2) {
+          const int o = (fy + 1) * RX + (cx + 2);  // region index of cell (gi, g)
+          auto B = [&](int var, int dxo, int dyo) { return double(W[var * PL + o + dxo + dyo * RX]); };
+          const double odx = 1.0 / a.dx;
+          const double eta_dx = eta_at(a.eta_kind, a.xc[gi], a.yc[g] + 0.5 * a.dx, 0.0) * odx;
+          const double JxS = eta_dx * (B(BZ, 0, 1) - B(BZ, 0, 0));
+          const double JzS = eta_dx * (0.25 * (B(BY, 1, 1) + B(BY, 1, 0) - B(BY, -1, 1) - B(BY, -1, 0)) -
+                                       (B(BX, 0, 1) - B(BX, 0, 0)));
+          Fo[EN] = T(double(Fo[EN]) + 0.5 * (JzS * (B(BX, 0, 0) + B(BX, 0, 1)) - JxS * (B(BZ, 0, 0) + B(BZ, 0, 1))));
+          Fo[BX] = T(double(Fo[BX]) + JzS);
+          Fo[BZ] = T(double(Fo[BZ]) - JxS);
+        }
       }
-    }
 #pragma unroll
-    for (int v = 0; v < NV; ++v) FB[v * SFLUX + q] = Fo[v];
+      for (int v = 0; v < NV; ++v) FBy[v * NYF + qq] = Fo[v];
+    }
   }
   __syncthreads();
 
-  // ---- G: update, ghost fill, GLM, CFL ----
-  const int gi = gi0 + tx, gj = gj0 + ty;
+  // ---- D: update, ghost fill, GLM, CFL ----
   double vcell = 0.0;
-  if (gi <= ix - 2 && gj <= jx - 2) {
-    const double dtx = a.dtx_scale * dt / a.dx, dty = a.dtx_scale * dt / a.dy;
-    const size_t c = (size_t)gi + (size_t)ix * gj;
-    double out[NV];
+  if (tid < TX * TY) {
+    const int tx = tid % TX, ty = tid / TX;
+    const int gi = gi0 + tx, gj = gj0 + ty;
+    if (gi <= ix - 2 && gj <= jx - 2) {
+      const double dtx = a.dtx_scale * dt / a.dx, dty = a.dtx_scale * dt / a.dy;
+      const size_t c = (size_t)gi + (size_t)ix * gj;
+      double out[NV];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      const double gm = double(FB[v * SFLUX + ty * TX + tx]), gp = double(FB[v * SFLUX + (ty + 1) * TX + tx]);
-      double d;
-      if (a.iso)
-        d = dtx * (acc[v] + gm - gp);  // rk.f90:26-35 operation order
-      else
-        d = dtx * acc[v] + dty * (gm - gp);
-      double ub = a.Ubase[v * N + c];
-      if (v == PS) ub = glmf * ub;
-      if (a.stage == 1 || a.time_type == OMHD_TIME_RK2)
-        out[v] = ub + d;  // rk_tvd21 / rk_std21 / rk_std22
-      else
-        out[v] = 0.5 * (ub + a.U1[v * N + c] + d);  // rk_tvd22 (rk.f90:56-66)
-    }
-    if (a.stage == 2) out[PS] = glmf * out[PS];  // second GLM half (main.f90:185)
-
-    // owner-writes ghost fill (bc.f90 order: x sides, then y sides)
-    int xt[3], yt[3], xf[3], yf[3], nxt = 1, nyt = 1;
-    xt[0] = gi; xf[0] = 0;
-    yt[0] = gj; yf[0] = 0;
-    if (gi == 1) { xt[nxt] = perx ? ix - 1 : 0; xf[nxt] = perx ? 0 : a.bc_flip[0]; ++nxt; }
-    if (gi == ix - 2) { xt[nxt] = perx ? 0 : ix - 1; xf[nxt] = perx ? 0 : a.bc_flip[1]; ++nxt; }
-    if (gj == 1) { yt[nyt] = pery ? jx - 1 : 0; yf[nyt] = pery ? 0 : a.bc_flip[2]; ++nyt; }
-    if (gj == jx - 2) { yt[nyt] = pery ? 0 : jx - 1; yf[nyt] = pery ? 0 : a.bc_flip[3]; ++nyt; }
-    for (int b = 0; b < nyt; ++b)
-      for (int q = 0; q < nxt; ++q) {
-        const size_t cc = (size_t)xt[q] + (size_t)ix * yt[b];
-        const int fm = xf[q] ^ yf[b];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) a.Uout[v * N + cc] = ((fm >> v) & 1) ? -out[v] : out[v];
+      for (int v = 0; v < NV; ++v) {
+        // F(i-1/2) - F(i+1/2) in FP64
+        const double dF = double(FBx[v * NXF + ty * XF + tx]) - double(FBx[v * NXF + ty * XF + tx + 1]);
+        const double gm = double(FBy[v * NYF + ty * TX + tx]), gp = double(FBy[v * NYF + (ty + 1) * TX + tx]);
+        double d;
+        if (a.iso)
+          d = dtx * (dF + gm - gp);  // rk.f90:26-35 operation order
+        else
+          d = dtx * dF + dty * (gm - gp);
+        double ub = a.Ubase[v * N + c];
+        if (v == PS) ub = glmf * ub;
+        if (a.stage == 1 || a.time_type == OMHD_TIME_RK2)
+          out[v] = ub + d;  // rk_tvd21 / rk_std21 / rk_std22
+        else
+          out[v] = 0.5 * (ub + a.U1[v * N + c] + d);  // rk_tvd22 (rk.f90:56-66)
       }
+      if (a.stage == 2) out[PS] = glmf * out[PS];  // second GLM half (main.f90:185)
 
-    if (a.stage == 2) {  // set_dt.f90:27-37 on the new state
-      const double ro = out[RO];
-      const double vx = div_<double, OMHD_FAST>(out[MX], ro), vy = div_<double, OMHD_FAST>(out[MY], ro), vz = div_<double, OMHD_FAST>(out[MZ], ro);
-      const double rv2 = vx * out[MX] + vy * out[MY] + vz * out[MZ];
-      const double B2 = out[BX] * out[BX] + out[BY] * out[BY] + out[BZ] * out[BZ];
-      const double pr = f1g * (out[EN] - 0.5 * (rv2 + B2));
-      const double f1 = gamma * pr;
-      const double vfx = fast_speed<double, OMHD_FAST>(f1, B2, out[BX], ro);
-      const double vfy = fast_speed<double, OMHD_FAST>(f1, B2, out[BY], ro);
-      vcell = fmax2(fabs(vx) + vfx, fabs(vy) + vfy);
+      // owner-writes ghost fill (bc.f90 order: x sides, then y sides)
+      int xt[3], yt[3], xf[3], yf[3], nxt = 1, nyt = 1;
+      xt[0] = gi;
+      xf[0] = 0;
+      yt[0] = gj;
+      yf[0] = 0;
+      if (gi == 1) { xt[nxt] = perx ? ix - 1 : 0; xf[nxt] = perx ? 0 : a.bc_flip[0]; ++nxt; }
+      if (gi == ix - 2) { xt[nxt] = perx ? 0 : ix - 1; xf[nxt] = perx ? 0 : a.bc_flip[1]; ++nxt; }
+      if (gj == 1) { yt[nyt] = pery ? jx - 1 : 0; yf[nyt] = pery ? 0 : a.bc_flip[2]; ++nyt; }
+      if (gj == jx - 2) { yt[nyt] = pery ? 0 : jx - 1; yf[nyt] = pery ? 0 : a.bc_flip[3]; ++nyt; }
+      for (int b = 0; b < nyt; ++b)
+        for (int q = 0; q < nxt; ++q) {
+          const size_t cc = (size_t)xt[q] + (size_t)ix * yt[b];
+          const int fm = xf[q] ^ yf[b];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) a.Uout[v * N + cc] = ((fm >> v) & 1) ? -out[v] : out[v];
+        }
+
+      if (a.stage == 2) {  // set_dt.f90:27-37 on the new state
+        const double ro = out[RO];
+        const double vx = div_<double, OMHD_FAST>(out[MX], ro), vy = div_<double, OMHD_FAST>(out[MY], ro),
+                     vz = div_<double, OMHD_FAST>(out[MZ], ro);
+        const double rv2 = vx * out[MX] + vy * out[MY] + vz * out[MZ];
+        const double B2 = out[BX] * out[BX] + out[BY] * out[BY] + out[BZ] * out[BZ];
+        const double pr = f1g * (out[EN] - 0.5 * (rv2 + B2));
+        const double f1 = gamma * pr;
+        const double vfx = fast_speed<double, OMHD_FAST>(f1, B2, out[BX], ro);
+        const double vfy = fast_speed<double, OMHD_FAST>(f1, B2, out[BY], ro);
+        vcell = fmax2(fabs(vx) + vfx, fabs(vy) + vfy);
+      }
     }
   }
+  return vcell;
+}
+
+// one CTA per tile of one grid
+template <class T, int FLUX>
+__global__ void __launch_bounds__(GeoDefault::NT) k_stage2d(const StageArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red32[32];
+  __shared__ int skip;
+  StepState* st = a.st;
+  // one thread decides, so that the whole CTA leaves together (the error word
+  // may be set by another CTA while this one starts)
+  if (threadIdx.x == 0) skip = st->done || *(volatile int*)&a.err->code;
+  __syncthreads();
+  if (skip) return;
+  const double vcell = stage2d_tile<T, FLUX, GeoDefault>(a, blockIdx.x, blockIdx.y, smem_raw, st->dt, st->ch,
+                                                         st->glm_f);
   if (a.stage == 2) {
     const double bm = block_max_pos(vcell, red32);
     StepConsts sc{a.cfl, a.dmin, a.dx, a.eta_kind};
@@ -314,18 +353,96 @@ __global__ void __launch_bounds__(NT) k_stage2d(const StageArgs a) {
   }
 }
 
+// Ensemble of independent 2D grids in one persistent launch: CTAs loop over
+// the tiles of all grids (work item w -> grid by binary search of the tile
+// prefix sums), each grid keeps its own dt, step record and error word, and
+// the CTA that finishes the last tile of a grid in stage 2 plans that grid's
+// next step.
+template <class T, int FLUX, class G>
+__global__ void __launch_bounds__(G::NT) k_batch2d(const StageArgs* __restrict__ args,
+                                                   const int* __restrict__ tile_start, int ngrids, int total_tiles) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red32[32];
+  __shared__ unsigned int is_last;
+  __shared__ int skip_s;
+  for (int w = blockIdx.x; w < total_tiles; w += gridDim.x) {
+    int lo = 0, hi = ngrids - 1;  // last grid with tile_start <= w
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tile_start[mid] <= w)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const StageArgs& a = args[lo];
+    StepState* st = a.st;
+    const int local = w - tile_start[lo];
+    const int ntx = (a.ix - 2 + G::TX - 1) / G::TX;
+    const int ntiles = ntx * ((a.jx - 2 + G::TY - 1) / G::TY);
+    if (threadIdx.x == 0) skip_s = st->done || *(volatile int*)&a.err->code;
+    __syncthreads();
+    const bool skip = skip_s;  // uniform over the CTA
+    double vcell = 0.0;
+    if (!skip) vcell = stage2d_tile<T, FLUX, G>(a, local % ntx, local / ntx, smem_raw, st->dt, st->ch, st->glm_f);
+    if (!skip && a.stage == 2) {
+      const double bm = block_max_pos(vcell, red32);
+      if (threadIdx.x == 0) {
+        atomic_max_pos_double(&st->vmax_acc, bm);
+        __threadfence();
+        is_last = (atomicAdd(&st->counter, 1u) == (unsigned)ntiles - 1) ? 1u : 0u;
+      }
+      __syncthreads();
+      if (is_last && threadIdx.x == 0) {
+        __threadfence();
+        StepConsts sc{a.cfl, a.dmin, a.dx, a.eta_kind};
+        finalize_step(st, sc, a.err, 1);
+      }
+    }
+    __syncthreads();  // shared memory is reused by the next work item
+  }
+}
+
 template <class T, int FLUX>
 int launch_one(const StageArgs& a, cudaStream_t s) {
-  const size_t bytes = smem2d_bytes<T>();
+  const size_t bytes = GeoDefault::smem_bytes<T>();
   static bool configured = false;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(k_stage2d<T, FLUX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e != cudaSuccess) return (int)e;
     configured = true;
   }
-  dim3 grid((a.ix - 2 + TX - 1) / TX, (a.jx - 2 + TY - 1) / TY);
-  k_stage2d<T, FLUX><<<grid, NT, bytes, s>>>(a);
+  dim3 grid((a.ix - 2 + GeoDefault::TX - 1) / GeoDefault::TX, (a.jx - 2 + GeoDefault::TY - 1) / GeoDefault::TY);
+  k_stage2d<T, FLUX><<<grid, GeoDefault::NT, bytes, s>>>(a);
   return (int)cudaGetLastError();
+}
+
+template <class T, int FLUX, class G>
+int launch_batch_one(const StageArgs* args_dev, const int* tile_start_dev, int ngrids, int total_tiles, int ctas,
+                     cudaStream_t s) {
+  const size_t bytes = G::template smem_bytes<T>();
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e =
+        cudaFuncSetAttribute(k_batch2d<T, FLUX, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return (int)e;
+    configured = true;
+  }
+  k_batch2d<T, FLUX, G><<<ctas, G::NT, bytes, s>>>(args_dev, tile_start_dev, ngrids, total_tiles);
+  return (int)cudaGetLastError();
+}
+
+// Batched launch with one of the tile shapes the ensemble autotuner chooses
+// from (HLLD only: the ensemble configuration's Riemann solver).
+template <class T>
+int launch_batch_variant(int flux, int tile_kind, const StageArgs* args, const int* tile_start, int ngrids,
+                         int total_tiles, int ctas, cudaStream_t s) {
+  if (flux != FX_HLLD) return (int)cudaErrorNotSupported;
+  switch (tile_kind) {
+    case 0: return launch_batch_one<T, FX_HLLD, Geo2<32, 8>>(args, tile_start, ngrids, total_tiles, ctas, s);
+    case 1: return launch_batch_one<T, FX_HLLD, Geo2<32, 4>>(args, tile_start, ngrids, total_tiles, ctas, s);
+    case 2: return launch_batch_one<T, FX_HLLD, Geo2<16, 16>>(args, tile_start, ngrids, total_tiles, ctas, s);
+    default: return launch_batch_one<T, FX_HLLD, Geo2<64, 4>>(args, tile_start, ngrids, total_tiles, ctas, s);
+  }
 }
 
 template <class T>

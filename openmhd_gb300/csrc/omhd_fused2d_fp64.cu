@@ -7,3 +7,10 @@
 namespace omhd {
 int launch_stage2d_fp64(const StageArgs& a, cudaStream_t s) { return v_fp64::launch_variant<double>(a, s); }
 }  // namespace omhd
+
+namespace omhd {
+int launch_batch2d_fp64(int flux, int tile_kind, const StageArgs* args_dev, const int* tile_start_dev, int ngrids,
+                      int total_tiles, int ctas, cudaStream_t s) {
+  return v_fp64::launch_batch_variant<double>(flux, tile_kind, args_dev, tile_start_dev, ngrids, total_tiles, ctas, s);
+}
+}  // namespace omhd

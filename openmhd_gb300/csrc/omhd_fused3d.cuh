@@ -115,9 +115,13 @@ __global__ void __launch_bounds__(NT) k_stage3d(const StageArgs a) {
   T* SR = SL + NV * SFACE;
   T* FB = SR + NV * SFACE;
   __shared__ double red32[32];
+  __shared__ int skip;
 
   StepState* st = a.st;
-  if (st->done || *(volatile int*)&a.err->code) return;
+  // one thread decides, so that the whole CTA leaves together
+  if (threadIdx.x == 0) skip = st->done || *(volatile int*)&a.err->code;
+  __syncthreads();
+  if (skip) return;
   const double dt = st->dt, chd = st->ch, glmf = st->glm_f;
   const int ix = a.ix, jx = a.jx, kx = a.kx;
   const size_t N = (size_t)ix * jx * kx;

@@ -106,6 +106,49 @@ __device__ __forceinline__ void reconstruct(int type, T wm, T w0, T wp, T& left,
   }
 }
 
+// Minimum of two non-negative doubles on the integer pipe: for x, y >= 0 the
+// order of the IEEE bit patterns is the numeric order.
+__device__ __forceinline__ double min_nonneg(double a, double b) {
+  const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+  return (ib < ia) ? b : a;  // same operand choice as fmin2(a, b)
+}
+
+// minmod and MC reconstruction for FP64 with the sign logic and the minimum
+// on the integer pipe.  (sign(c,gA)+sign(c,gB)) is 0 when the signs differ and
+// +-2c otherwise, and 2c*min(...) is an exact power-of-two scaling, so the face
+// states equal the reference's bit for bit: w0 +- (+-2c)*m is one fused
+// multiply-add with an exactly representable product.
+template <bool FAST>
+__device__ __forceinline__ void reconstruct_fp64(int type, double wm, double w0, double wp, double& left,
+                                                 double& right) {
+  if constexpr (FAST) {
+    if (type == LM_MINMOD || type == LM_MC) {
+      const double gA = (w0 - wm);
+      const double gB = (wp - w0);
+      const long long sa = __double_as_longlong(gA), sb = __double_as_longlong(gB);
+      double m = min_nonneg(fabs(gA), fabs(gB));
+      double c = 0.5;  // minmod: (0.25 + 0.25)
+      if (type == LM_MC) {
+        m = min_nonneg(m, fabs(0.25 * (wp - wm)));
+        c = 1.0;  // MC: (0.5 + 0.5)
+      }
+      const double s = ((sa ^ sb) < 0) ? 0.0 : copysign(c, gA);
+      left = fma(s, m, w0);
+      right = fma(-s, m, w0);
+      return;
+    }
+  }
+  reconstruct<double>(type, wm, w0, wp, left, right);
+}
+
+template <class T, bool FAST>
+__device__ __forceinline__ void reconstruct_t(int type, T wm, T w0, T wp, T& left, T& right) {
+  if constexpr (sizeof(T) == 8)
+    reconstruct_fp64<FAST>(type, wm, w0, wp, left, right);
+  else
+    reconstruct<T>(type, wm, w0, wp, left, right);
+}
+
 // Numerical flux across one face (2D_basic/flux_solver.f90):
 //   LLF :89-148, HLL :153-221, HLLC :226-347, HLLD :352-585 (HLLC-G fallback
 //   :447-476), LHLLD :590-789; GLM fluxes for Bn and psi :580-581.

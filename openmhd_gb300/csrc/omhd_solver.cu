@@ -10,6 +10,7 @@
 #include "omhd_common.cuh"
 #include "omhd_fused.h"
 #include "omhd_riemann.cuh"
+#include "omhd_solver_impl.h"
 #include "omhd_step.cuh"
 
 namespace omhd {
@@ -159,26 +160,44 @@ __global__ void k_set_tend(StepState* st, double tend) {
 
 using namespace omhd;
 
-struct omhd_solver {
-  omhd_config cfg;
-  size_t n = 0;  // cells per variable plane
-  double* U = nullptr;
-  double* U1 = nullptr;
-  bool own_state = false;
-  double* xc = nullptr;  // device coordinates
-  double* yc = nullptr;
-  double* zc = nullptr;
-  std::vector<double> hx, hy, hz;
-  StepState* st = nullptr;
-  DevError* err = nullptr;
-  cudaStream_t stream = nullptr;
-  cudaGraphExec_t graph = nullptr;
-  int graph_steps = 0;
-  int iso = 1;
-  double dmin = 0;
-  int last_status = OMHD_OK;
-  omhd_error_info last = {};
-};
+namespace omhd {
+StageArgs make_stage_args(const omhd_solver* s, int stage) {
+  StageArgs a;
+  memset(&a, 0, sizeof a);
+  const omhd_config& c = s->cfg;
+  a.Uin = (stage == 1) ? s->U : s->U1;
+  a.Ubase = s->U;
+  a.U1 = (stage == 2) ? s->U1 : nullptr;
+  a.Uout = (stage == 1) ? s->U1 : s->U;
+  a.ix = c.ix;
+  a.jx = c.jx;
+  a.kx = c.kx;
+  a.nd = c.nd;
+  a.dx = c.dx;
+  a.dy = c.dy;
+  a.dz = c.nd == 3 ? c.dz : c.dx;
+  a.dtx_scale = (stage == 1 && c.time_type == OMHD_TIME_RK2) ? 0.5 : 1.0;
+  a.gamma = c.gamma;
+  a.lm_type = c.lm_type;
+  a.flux_type = c.flux_type;
+  a.time_type = c.time_type;
+  a.stage = stage;
+  a.iso = s->iso;
+  for (int q = 0; q < 6; ++q) {
+    a.bc_kind[q] = c.bc_kind[q];
+    a.bc_flip[q] = c.bc_flip[q];
+  }
+  a.eta_kind = c.eta_kind;
+  a.xc = s->xc;
+  a.yc = s->yc;
+  a.zc = s->zc;
+  a.st = s->st;
+  a.err = s->err;
+  a.cfl = c.cfl;
+  a.dmin = s->dmin;
+  return a;
+}
+}  // namespace omhd
 
 namespace {
 
@@ -214,39 +233,8 @@ StepConsts consts_of(const omhd_solver* s) {
 }
 
 int launch_stage(omhd_solver* s, int stage) {
-  StageArgs a;
-  memset(&a, 0, sizeof a);
+  const StageArgs a = make_stage_args(s, stage);
   const omhd_config& c = s->cfg;
-  a.Uin = (stage == 1) ? s->U : s->U1;
-  a.Ubase = s->U;
-  a.U1 = (stage == 2) ? s->U1 : nullptr;
-  a.Uout = (stage == 1) ? s->U1 : s->U;
-  a.ix = c.ix;
-  a.jx = c.jx;
-  a.kx = c.kx;
-  a.nd = c.nd;
-  a.dx = c.dx;
-  a.dy = c.dy;
-  a.dz = c.nd == 3 ? c.dz : c.dx;
-  a.dtx_scale = (stage == 1 && c.time_type == OMHD_TIME_RK2) ? 0.5 : 1.0;
-  a.gamma = c.gamma;
-  a.lm_type = c.lm_type;
-  a.flux_type = c.flux_type;
-  a.time_type = c.time_type;
-  a.stage = stage;
-  a.iso = s->iso;
-  for (int q = 0; q < 6; ++q) {
-    a.bc_kind[q] = c.bc_kind[q];
-    a.bc_flip[q] = c.bc_flip[q];
-  }
-  a.eta_kind = c.eta_kind;
-  a.xc = s->xc;
-  a.yc = s->yc;
-  a.zc = s->zc;
-  a.st = s->st;
-  a.err = s->err;
-  a.cfl = c.cfl;
-  a.dmin = s->dmin;
   int e;
   if (c.nd == 2) {
     if (c.precision == OMHD_PREC_FP64)

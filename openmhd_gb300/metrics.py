@@ -19,13 +19,15 @@ def rel_l1(a: np.ndarray, b: np.ndarray) -> np.ndarray:
 def scaled_l1(a: np.ndarray, b: np.ndarray) -> np.ndarray:
     """Per-variable L1 error of a against b, each variable normalised by the L1
     norm of its physical scale: rho and E by themselves, the momentum
-    components by |m|, the field components and psi by |B|.  Components that
-    are ~0 (By, vy, psi early in a run) are measured against the magnitude of
-    the vector they belong to, not against their own round-off."""
+    components by sqrt(2 rho E) (>= |m|, the momentum a cell's total energy
+    could carry), the field components and psi by |B|.  Components that are
+    ~0 (By, vy, psi early in a run, momentum of a static equilibrium) are
+    measured against the scale of the state, not against their own
+    round-off."""
     a = a.reshape(a.shape[0], -1)
     b = b.reshape(b.shape[0], -1)
     num = np.abs(a - b).sum(axis=1)
-    m = np.sqrt((b[0:3] ** 2).sum(axis=0)).sum()
+    m = np.sqrt(np.abs(2.0 * b[4] * b[3])).sum()
     B = np.sqrt((b[5:8] ** 2).sum(axis=0)).sum()
     den = np.array([m, m, m, np.abs(b[3]).sum(), np.abs(b[4]).sum(), B, B, B, B])
     floor = max(den.max(), 1e-300) * 1e-12
