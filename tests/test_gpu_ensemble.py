@@ -1,14 +1,19 @@
-"""Batched ensemble: every member of one persistent launch must evolve exactly
-as the same problem run alone by the single-grid solver (tiling never changes
-the arithmetic of a cell, and each member keeps its own dt)."""
+"""Batched ensemble: every member of one persistent launch must evolve as the
+same problem run alone by the single-grid solver.  The two are different
+kernels built from the same source; with multiply-add contraction on, the
+compiler may contract differently in each, so they agree to rounding (FP64
+1e-12, FP32-mixed 1e-6 scaled L1), while two ensemble runs with different
+launch paths (stream vs graph) agree bit for bit."""
 import numpy as np
 import pytest
+
+from helpers import scaled_l1
 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("precision", ["mixed", "fp64"])
-def test_members_match_single_grid_runs(cuda_lib, precision):
+@pytest.mark.parametrize("precision,tol", [("mixed", 1e-6), ("fp64", 1e-12)])
+def test_members_match_single_grid_runs(cuda_lib, precision, tol):
     from openmhd_gb300 import Solver
     from openmhd_gb300.ensemble import Ensemble, batched_problem_set
 
@@ -24,8 +29,9 @@ def test_members_match_single_grid_runs(cuda_lib, precision):
         ref = s.get_state_numpy()
         info = s.sync()
         assert infos[i].steps == info.steps
-        assert infos[i].t == info.t
-        assert np.array_equal(ens.member_state(i), ref), i
+        assert abs(infos[i].t - info.t) <= tol * info.t
+        err = scaled_l1(ens.member_state(i)[:, 1:-1, 1:-1], ref[:, 1:-1, 1:-1])
+        assert np.all(err <= tol), (i, err)
 
 
 def test_graph_replay_and_per_member_dt(cuda_lib):
