@@ -309,6 +309,8 @@ def run_ours(args):
     }
     if not args.no_batched:
         line["batched"] = run_batched(args)
+    if not args.no_adjoint:
+        line["adjoint"] = run_adjoint(args)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"], _ = cpu_baseline(steps_budget_s=10.0)
     if rank == 0:
@@ -364,6 +366,118 @@ def run_batched(args):
             "dt_range": [min(x.dt for x in infos), max(x.dt for x in infos)]}
 
 
+ADJ_NX, ADJ_NY, ADJ_STEPS, ADJ_EVERY = 512, 256, 400, 20
+
+
+def run_adjoint(args, ndir: int = 16, eps: float = 1e-6):
+    """Gradient through time: KH 512 x 256 FP64, 400 TVD-RK2 steps (HLLD +
+    minmod + GLM), J = sum By^2 at the final time, dJ/dvy0 over the full
+    interior vy0 field through the hand-written adjoint kernels behind a
+    torch.autograd.Function, checkpoint every 20 steps.  Reports forward and
+    backward time, the time of one adjoint step against one forward step,
+    device memory, and central finite differences of J (eps = 1e-6) along
+    seeded random directions."""
+    import numpy as np
+    import torch
+
+    from openmhd_gb300 import Solver, kelvin_helmholtz
+    from openmhd_gb300.adjoint import AdjointRun, Evolve, kh_state
+
+    cfg, model = kelvin_helmholtz(ADJ_NX, ADJ_NY, precision="fp64")
+    s = Solver(cfg).init_model(model)
+    base = s.U.clone()
+    torch.cuda.synchronize()
+    run = AdjointRun(cfg, ADJ_STEPS, ADJ_EVERY)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def timed(stream, fn):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    # plain forward: the fused solver alone (warm once)
+    s.step(3)
+    s.sync()
+    s.put_state(base)
+    t_fwd = timed(s.stream, lambda: s.step(ADJ_STEPS))
+    s.sync()
+
+    def objective(vy):
+        UN = Evolve.apply(kh_state(base, vy), run)
+        return (UN[6, 1:-1, 1:-1] ** 2).sum()
+
+    vy0 = (base[1, 1:-1, 1:-1] / base[4, 1:-1, 1:-1]).clone()
+    vy = vy0.clone().requires_grad_(True)
+    J = objective(vy)  # warm-up forward + backward
+    J.backward()
+    torch.cuda.reset_peak_memory_stats()
+    vy = vy0.clone().requires_grad_(True)
+    U0 = kh_state(base, vy)
+    UN_holder = {}
+    t_fwd_ck = timed(run.stream, lambda: UN_holder.update(UN=Evolve.apply(U0, run)))
+    J = (UN_holder["UN"][6, 1:-1, 1:-1] ** 2).sum()
+    t_bwd = timed(run.stream, lambda: J.backward())
+    run.sync()
+    grad = vy.grad.detach().clone()
+    peak_torch = torch.cuda.max_memory_allocated()
+
+    # one adjoint step against one forward step, on stored stage inputs
+    s.put_state(base)
+    s.step(5)
+    s.sync()
+    Un = s.U.clone()
+    s.step(1)
+    s.sync()
+    U1 = s.U1.clone()
+    log3 = torch.tensor(run.step_log()[5], dtype=torch.float64, device="cuda")
+    lam = torch.randn(cfg.shape, dtype=torch.float64, device="cuda")
+    lam_out = torch.empty_like(lam)
+    reps = 50
+    run.step_vjp(Un, U1, log3, lam.clone(), lam_out)
+    t_vjp = timed(run.stream, lambda: [run.step_vjp(Un, U1, log3, lam, lam_out) for _ in range(reps)]) / reps
+    t_step = timed(s.stream, lambda: s.step(reps)) / reps
+
+    # central finite differences along seeded directions
+    y = torch.from_numpy(s.coords()[1][1:-1]).cuda()
+    env = torch.exp(-y * y)[:, None]
+    gen = torch.Generator(device="cuda").manual_seed(1234)
+    rows = []
+    with torch.no_grad():
+        for k in range(ndir + 4):
+            d = torch.randn(tuple(vy0.shape), dtype=torch.float64, device="cuda", generator=gen)
+            kind = "kh_envelope" if k < ndir else "full_field"
+            if kind == "kh_envelope":
+                d = d * env
+            jp = float(objective(vy0 + eps * d))
+            jm = float(objective(vy0 - eps * d))
+            fd = (jp - jm) / (2 * eps)
+            ad = float((grad * d).sum())
+            rows.append((kind, fd, ad, abs(fd - ad) / max(abs(fd), 1e-300)))
+    env_err = [r[3] for r in rows if r[0] == "kh_envelope"]
+    full_err = [r[3] for r in rows if r[0] == "full_field"]
+    run.sync()
+    return {
+        "workload": f"kh2d_{ADJ_NX}x{ADJ_NY}_fp64_{ADJ_STEPS}steps_adjoint_J=sum(By^2)_d/dvy0",
+        "steps": ADJ_STEPS, "checkpoint_every": ADJ_EVERY, "J": float(J),
+        "forward_s": t_fwd, "forward_with_checkpoints_s": t_fwd_ck, "backward_s": t_bwd,
+        "backward_over_forward": t_bwd / t_fwd,
+        "adjoint_step_ms": 1e3 * t_vjp, "forward_step_ms": 1e3 * t_step,
+        "adjoint_step_over_forward_step": t_vjp / t_step,
+        "adjoint_launches_per_step": 6,
+        "device_bytes_adjoint_handle": run.memory_bytes, "device_bytes_torch_peak": int(peak_torch),
+        "state_bytes": 9 * cfg.ix * cfg.jx * 8,
+        "fd": {"eps": eps, "directions": ndir, "max_rel_err": max(env_err), "median_rel_err": float(np.median(env_err)),
+               "direction_kind": "seeded N(0,1) per cell times exp(-y^2) (the perturbation's envelope)",
+               "full_field_max_rel_err": max(full_err),
+               "samples": [[r[0], r[1], r[2]] for r in rows[:3]]},
+        "grad_norm": float(grad.norm()),
+    }
+
+
 def _fp64_peak_gflops(lib) -> float:
     import ctypes as C
 
@@ -408,6 +522,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-only", action="store_true", help="run the adjoint leg alone")
     ap.add_argument("--profile", action="store_true", help="small fixed run for profiler captures")
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
@@ -427,6 +543,9 @@ def main():
     from oracle import oracle
 
     build()
+    if args.adjoint_only:
+        print(json.dumps({"adjoint": run_adjoint(args)}), flush=True)
+        return 0
     oracle.build()
     return run_ours(args)
 

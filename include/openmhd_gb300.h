@@ -308,6 +308,40 @@ int omhd_step2d_noalloc(double* U_dev, const omhd_config* cfg, double t0, int ns
                         omhd_step_info* info);
 size_t omhd_step2d_noalloc_max_doubles(void);
 
+/* ======================================================================
+ * Reverse mode through time (no counterpart in the reference).  The
+ * gradient of a scalar functional J(U_N) with respect to the initial state
+ * U_0 of `nsteps` fused FP64 TVD-RK2 steps (2D, HLLD, minmod or MC, GLM,
+ * periodic or mirror boundaries).  Hand-written adjoint kernels per RK stage
+ * recompute each face's HLLD branch and limiter selection from the stored
+ * stage inputs (a fixed subgradient at limiter kinks); dt and ch of every
+ * step are recorded by the forward run and held fixed.  States are kept
+ * every `checkpoint_every` steps; the backward pass recomputes one segment
+ * of steps at a time (sqrt(N) checkpointing when checkpoint_every ~ sqrt(N)).
+ * Arrays are device memory in the reference layout (9 planes of ix*jx).
+ * ==================================================================== */
+typedef struct omhd_adjoint omhd_adjoint;
+/* cfg: nd = 2, flux HLLD, limiter minmod or MC, TVD-RK2, no resistivity;
+ * the precision field is ignored (the forward runs the fp64 kernels). */
+int omhd_adjoint_create(const omhd_config* cfg, int nsteps, int checkpoint_every, omhd_adjoint** out);
+int omhd_adjoint_destroy(omhd_adjoint* a);
+int omhd_adjoint_set_stream(omhd_adjoint* a, void* cuda_stream);
+/* bc is applied to a copy of U0 (U0 is not modified); U_N goes to UN (may be NULL) */
+int omhd_adjoint_forward(omhd_adjoint* a, const double* U0_dev, double* UN_dev);
+/* gU0 = (dU_N/dU_0)^T gUN, zero at ghost cells; needs a preceding forward */
+int omhd_adjoint_backward(omhd_adjoint* a, const double* gUN_dev, double* gU0_dev);
+/* adjoint of one step given its stage inputs Un (before the first GLM half)
+ * and U1 (after bc); log3_dev = {dt, ch, glm factor} on the device.  lam_in
+ * is dJ/dU_{n+1}; it is overwritten (its boundary ring folds in the ghosts). */
+int omhd_adjoint_step_vjp(omhd_adjoint* a, const double* Un_dev, const double* U1_dev, const double* log3_dev,
+                          double* lam_in_dev, double* lam_out_dev);
+/* waits; returns the first device-reported failure of the forward steps */
+int omhd_adjoint_sync(omhd_adjoint* a);
+/* {dt, ch, glm factor} of each step of the last forward run (3*nsteps doubles) */
+int omhd_adjoint_step_log(omhd_adjoint* a, double* log3_host);
+/* device bytes held by the handle (checkpoints, segment and work buffers) */
+int omhd_adjoint_memory(omhd_adjoint* a, size_t* bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -122,6 +122,15 @@ SIGNATURES = [
     ("omhd_ensemble_sync", I, [P, C.POINTER(StepInfo)]),
     ("omhd_step2d_noalloc", I, [P, C.POINTER(Config), D, I, P, C.POINTER(StepInfo)]),
     ("omhd_step2d_noalloc_max_doubles", C.c_size_t, []),
+    ("omhd_adjoint_create", I, [C.POINTER(Config), I, I, C.POINTER(C.c_void_p)]),
+    ("omhd_adjoint_destroy", I, [P]),
+    ("omhd_adjoint_set_stream", I, [P, P]),
+    ("omhd_adjoint_forward", I, [P, P, P]),
+    ("omhd_adjoint_backward", I, [P, P, P]),
+    ("omhd_adjoint_step_vjp", I, [P, P, P, P, P, P]),
+    ("omhd_adjoint_sync", I, [P]),
+    ("omhd_adjoint_step_log", I, [P, P]),
+    ("omhd_adjoint_memory", I, [P, C.POINTER(C.c_size_t)]),
 ]
 
 

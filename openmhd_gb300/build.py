@@ -34,6 +34,7 @@ UNITS = {
     "omhd_fused3d_mixed.cu": ["--fmad=true"],
     "omhd_noalloc.cu": [],
     "omhd_ensemble.cu": [],
+    "omhd_adjoint.cu": ["--fmad=true"],
 }
 
 

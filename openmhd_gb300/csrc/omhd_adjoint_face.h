@@ -652,7 +652,8 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
     gsqR -= gaVR * aVR / sqR;
     groL += (sqL > 0.0) ? gsqL * 0.5 / sqL : 0.0;
     groR += (sqR > 0.0) ? gsqR * 0.5 / sqR : 0.0;
-    gUh[bn] += gaUbn * std::copysign(1.0, Ubn);
+    // d|Bn|/dBn: the sign, and 0 at Bn == 0 (where a central difference sees no slope)
+    gUh[bn] += (Ubn > 0.0) ? gaUbn : ((Ubn < 0.0) ? -gaUbn : 0.0);
     gL[kRO] += groL * tL / eL;
     gtL += groL * L[kRO] / eL;
     geL -= groL * roL / eL;

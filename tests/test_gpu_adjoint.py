@@ -1,0 +1,145 @@
+"""Hand-written adjoint of the fused FP64 2D step on the GPU.
+
+- forward of the adjoint handle == the fused solver, bit for bit;
+- dJ/dU0 of a few steps == PyTorch autograd of the pure-torch reference step
+  (same dt, ch, GLM factor), for periodic, zero-gradient and sign-flipping
+  walls, minmod and MC;
+- checkpoint spacing does not change the gradient (bit for bit);
+- KH dJ/dvy0 with J = sum By^2 agrees with central finite differences of
+  the forward along seeded directions.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import torch_ref_step as tr
+from helpers import smooth_state
+
+pytestmark = pytest.mark.gpu
+
+BCS = {
+    "periodic_mc": ("mc", (0, 0, 0, 0, 0, 0), (0,) * 6),
+    "kh_walls_minmod": ("minmod", (0, 0, 1, 1, 0, 0), (0,) * 6),
+    "flip_walls_minmod": ("minmod", (1, 1, 1, 1, 0, 0), (0b010000001, 0b010000001, 0b001000010, 0b001000010, 0, 0)),
+}
+
+
+def small_cfg(name, ix=26, jx=20, dx=0.3, dy=0.25):
+    from openmhd_gb300 import SolverConfig
+
+    lim, bk, bf = BCS[name]
+    return SolverConfig(nd=2, ix=ix, jx=jx, dx=dx, dy=dy, limiter=lim, flux="hlld", bc_kind=bk, bc_flip=bf)
+
+
+def test_adjoint_forward_matches_solver(cuda_lib):
+    from openmhd_gb300 import Solver
+    from openmhd_gb300.adjoint import AdjointRun
+
+    cfg = small_cfg("kh_walls_minmod", 70, 38)
+    U0 = smooth_state(38, 70, 1)
+    s = Solver(cfg).put_state(U0)
+    s.step(7)
+    ref = s.get_state_numpy()
+    run = AdjointRun(cfg, 7, 3)
+    UN = run.forward(torch.from_numpy(U0)).cpu().numpy()
+    run.sync()
+    assert np.array_equal(UN, ref)
+    assert run.step_log().shape == (7, 3)
+
+
+@pytest.mark.parametrize("name", sorted(BCS))
+def test_gradient_matches_torch_autograd(cuda_lib, name):
+    from openmhd_gb300.adjoint import AdjointRun
+
+    cfg = small_cfg(name)
+    nsteps = 3
+    U0 = torch.from_numpy(smooth_state(cfg.jx, cfg.ix, 7))
+    run = AdjointRun(cfg, nsteps, 2)
+    UN = run.forward(U0).cpu()
+    run.sync()
+    log = run.step_log()
+    rng = np.random.default_rng(3)
+    gUN = torch.from_numpy(rng.standard_normal(cfg.shape))
+    g_gpu = run.backward(gUN.cuda()).cpu().numpy()
+    run.sync()
+
+    U0t = U0.clone().requires_grad_(True)
+    UNt = tr.evolve(U0t, log, cfg)
+    assert torch.allclose(UNt.detach(), UN, rtol=0, atol=1e-12 * float(UN.abs().max()))
+    (UNt * gUN).sum().backward()
+    g_ref = U0t.grad.numpy()
+    scale = np.abs(g_ref).max()
+    err = np.abs(g_gpu - g_ref).max(axis=(1, 2)) / scale
+    assert np.all(err < 1e-11), err
+    # ghost entries of the gradient are zero: bc overwrites the input ghosts
+    assert np.all(g_gpu[:, 0, :] == 0) and np.all(g_gpu[:, :, -1] == 0)
+
+
+def test_checkpoint_spacing_is_exact(cuda_lib):
+    from openmhd_gb300.adjoint import AdjointRun
+
+    cfg = small_cfg("periodic_mc", 34, 30)
+    U0 = torch.from_numpy(smooth_state(cfg.jx, cfg.ix, 2)).cuda()
+    gUN = torch.from_numpy(np.random.default_rng(0).standard_normal(cfg.shape)).cuda()
+    grads = []
+    for every in (1, 3, 10):
+        run = AdjointRun(cfg, 10, every)
+        run.forward(U0)
+        grads.append(run.backward(gUN).cpu().numpy())
+        run.sync()
+    assert np.array_equal(grads[0], grads[1]) and np.array_equal(grads[0], grads[2])
+
+
+def kh_objective(run, base, vy):
+    from openmhd_gb300.adjoint import Evolve, kh_state
+
+    U0 = kh_state(base, vy)
+    UN = Evolve.apply(U0, run)
+    return (UN[6, 1:-1, 1:-1] ** 2).sum()
+
+
+def test_kh_gradient_against_finite_differences(cuda_lib):
+    """dJ/dvy0 against central differences of the forward.  The scheme is
+    piecewise smooth (limiter selections, HLLD branches), so a difference
+    that straddles a kink is not a derivative; the step is small enough
+    (1e-8, in the perturbation's exp(-y^2) envelope) that no face of these
+    5 steps changes branch, and the gap then is rounding only."""
+    from openmhd_gb300 import Solver, kelvin_helmholtz
+    from openmhd_gb300.adjoint import AdjointRun
+
+    cfg, model = kelvin_helmholtz(64, 32, precision="fp64")
+    base = torch.from_numpy(Solver(cfg).init_model(model).get_state_numpy()).cuda()
+    vy0 = (base[1, 1:-1, 1:-1] / base[4, 1:-1, 1:-1]).clone()
+    run = AdjointRun(cfg, 5, 2)
+    vy = vy0.clone().requires_grad_(True)
+    J = kh_objective(run, base, vy)
+    J.backward()
+    grad = vy.grad.detach()
+    assert torch.isfinite(grad).all() and float(grad.abs().max()) > 0
+    ycen = torch.from_numpy(Solver(cfg).coords()[1][1:-1]).cuda()
+    rng = np.random.default_rng(11)
+    eps = 1e-8
+    worst = 0.0
+    for _ in range(4):
+        d = torch.from_numpy(rng.standard_normal(tuple(vy0.shape))).cuda() * torch.exp(-ycen**2)[:, None]
+        with torch.no_grad():
+            jp = kh_objective(run, base, vy0 + eps * d)
+            jm = kh_objective(run, base, vy0 - eps * d)
+        fd = float((jp - jm) / (2 * eps))
+        ad = float((grad * d).sum())
+        worst = max(worst, abs(fd - ad) / max(abs(fd), 1e-300))
+    assert worst < 1e-6, worst
+
+
+def test_memory_report(cuda_lib):
+    from openmhd_gb300.adjoint import AdjointRun
+
+    cfg = small_cfg("periodic_mc", 34, 30)
+    run = AdjointRun(cfg, 100, 10)
+    S = 9 * cfg.ix * cfg.jx * 8
+    # 10 checkpoints + 2 x 10 segment states + 10 state-sized work arrays + step log
+    assert run.memory_bytes >= S * (10 + 20 + 10) + 3 * 100 * 8
+    assert run.memory_bytes < S * (10 + 20 + 10) + 3 * 100 * 8 + 4096
+    assert math.isfinite(run.memory_bytes)
