@@ -313,11 +313,12 @@ size_t omhd_step2d_noalloc_max_doubles(void);
  * gradient of a scalar functional J(U_N) with respect to the initial state
  * U_0 of `nsteps` fused FP64 TVD-RK2 steps (2D, HLLD, minmod or MC, GLM,
  * periodic or mirror boundaries).  Hand-written adjoint kernels per RK stage
- * recompute each face's HLLD branch and limiter selection from the stored
- * stage inputs (a fixed subgradient at limiter kinks); dt and ch of every
- * step are recorded by the forward run and held fixed.  States are kept
- * every `checkpoint_every` steps; the backward pass recomputes one segment
- * of steps at a time (sqrt(N) checkpointing when checkpoint_every ~ sqrt(N)).
+ * replay each face's HLLD branch and each limiter selection as the forward
+ * took them (a fixed subgradient at limiter kinks); dt and ch of every step
+ * are recorded by the forward run and held fixed.  States are kept every
+ * `checkpoint_every` steps; the backward pass recomputes one segment of
+ * steps at a time with the fused kernels, recording that segment's decision
+ * tape (sqrt(N) checkpointing when checkpoint_every ~ sqrt(N)).
  * Arrays are device memory in the reference layout (9 planes of ix*jx).
  * ==================================================================== */
 typedef struct omhd_adjoint omhd_adjoint;
@@ -330,9 +331,18 @@ int omhd_adjoint_set_stream(omhd_adjoint* a, void* cuda_stream);
 int omhd_adjoint_forward(omhd_adjoint* a, const double* U0_dev, double* UN_dev);
 /* gU0 = (dU_N/dU_0)^T gUN, zero at ghost cells; needs a preceding forward */
 int omhd_adjoint_backward(omhd_adjoint* a, const double* gUN_dev, double* gU0_dev);
+/* forward run that also records every step's decision tape (limiter
+ * selections and HLLD branches; about 44 bytes per cell per step), then
+ * replayed by omhd_adjoint_replay: the same steps from another U0 with every
+ * decision and every {dt, ch, glm factor} frozen to the recorded run's -- the
+ * smooth map whose derivative omhd_adjoint_backward computes (finite
+ * differences of it straddle no limiter or branch kink). */
+int omhd_adjoint_record(omhd_adjoint* a, const double* U0_dev, double* UN_dev);
+int omhd_adjoint_replay(omhd_adjoint* a, const double* U0_dev, double* UN_dev);
 /* adjoint of one step given its stage inputs Un (before the first GLM half)
- * and U1 (after bc); log3_dev = {dt, ch, glm factor} on the device.  lam_in
- * is dJ/dU_{n+1}; it is overwritten (its boundary ring folds in the ghosts). */
+ * and U1 (after bc); log3_dev = {dt, ch, glm factor} on the device; the
+ * decisions are recomputed from Un and U1.  lam_in is dJ/dU_{n+1}; it is
+ * overwritten (its boundary ring folds in the ghosts). */
 int omhd_adjoint_step_vjp(omhd_adjoint* a, const double* Un_dev, const double* U1_dev, const double* log3_dev,
                           double* lam_in_dev, double* lam_out_dev);
 /* waits; returns the first device-reported failure of the forward steps */

@@ -127,6 +127,8 @@ SIGNATURES = [
     ("omhd_adjoint_set_stream", I, [P, P]),
     ("omhd_adjoint_forward", I, [P, P, P]),
     ("omhd_adjoint_backward", I, [P, P, P]),
+    ("omhd_adjoint_record", I, [P, P, P]),
+    ("omhd_adjoint_replay", I, [P, P, P]),
     ("omhd_adjoint_step_vjp", I, [P, P, P, P, P, P]),
     ("omhd_adjoint_sync", I, [P]),
     ("omhd_adjoint_step_log", I, [P, P]),

@@ -69,14 +69,7 @@ class AdjointRun:
 
     def forward(self, U0):
         """U_N of nsteps steps from U0 (bc is applied to a copy of U0)."""
-        src = self._as_state(U0)
-        out = torch.empty(self.cfg.shape, dtype=torch.float64, device="cuda")
-        self.stream.wait_stream(torch.cuda.current_stream())
-        self._check(self.lib.omhd_adjoint_forward(self._h, src.data_ptr(), out.data_ptr()), "adjoint forward failed")
-        src.record_stream(self.stream)
-        out.record_stream(self.stream)
-        torch.cuda.current_stream().wait_stream(self.stream)
-        return out
+        return self._run(self.lib.omhd_adjoint_forward, U0, "adjoint forward failed")
 
     def backward(self, gUN):
         """dJ/dU0 given dJ/dU_N (zero at ghost cells)."""
@@ -88,6 +81,26 @@ class AdjointRun:
         out.record_stream(self.stream)
         torch.cuda.current_stream().wait_stream(self.stream)
         return out
+
+    def _run(self, fn, U0, what):
+        src = self._as_state(U0)
+        out = torch.empty(self.cfg.shape, dtype=torch.float64, device="cuda")
+        self.stream.wait_stream(torch.cuda.current_stream())
+        self._check(fn(self._h, src.data_ptr(), out.data_ptr()), what)
+        src.record_stream(self.stream)
+        out.record_stream(self.stream)
+        torch.cuda.current_stream().wait_stream(self.stream)
+        return out
+
+    def record(self, U0):
+        """forward(U0) that also records every step's decision tape (limiter
+        selections, HLLD branches) for replay()."""
+        return self._run(self.lib.omhd_adjoint_record, U0, "adjoint record failed")
+
+    def replay(self, U0):
+        """U_N from U0 with every decision and every dt, ch, GLM factor frozen
+        to the last record() run: the smooth map the adjoint differentiates."""
+        return self._run(self.lib.omhd_adjoint_replay, U0, "adjoint replay failed")
 
     def step_vjp(self, Un, U1, log3, lam_in, lam_out):
         """Adjoint of one step given its stage inputs (device tensors); lam_in is overwritten."""

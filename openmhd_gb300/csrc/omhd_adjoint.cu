@@ -19,10 +19,13 @@
 //   k_adj_prim  (Ua)   primitives of Ua; bc adjoint of lam1
 //   k_adj_faces (Ua)   g_F = dt/dx (lam1_{i+1} - lam1_i)
 //   k_adj_cells (Ua)   lam^n = 0.5 lam + lam1 (interior) + stage adjoint; psi *= f
-// HLLD branches and limiter selections are recomputed from the stored stage
-// inputs, so they are exactly the forward's; at a limiter kink the adjoint
-// takes the branch the forward took (a fixed subgradient).  dt and ch are
-// the forward's recorded values, held fixed.
+// The HLLD branches and limiter selections are the forward's: the backward
+// pass recomputes each checkpoint segment with the fused stage kernels in
+// tape-recording mode (omhd_tape.h) and the adjoint kernels replay those
+// decisions, so at a limiter kink the adjoint takes the branch the forward
+// took (a fixed subgradient).  dt and ch are the forward's recorded values,
+// held fixed.  A full-length tape also drives a frozen-decision forward
+// (omhd_adjoint_replay): the smooth map whose derivative the adjoint is.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -30,9 +33,11 @@
 
 #include "omhd_adjoint_face.h"
 #include "omhd_common.cuh"
+#include "omhd_fused.h"
 #include "omhd_riemann.cuh"
 #include "omhd_solver_impl.h"
 #include "omhd_step.cuh"
+#include "omhd_tape.h"
 
 namespace omhd {
 namespace {
@@ -131,9 +136,12 @@ __global__ void __launch_bounds__(256) k_adj_prim(AdjGeo g, const double* __rest
 // face fixes of bc.f90 folded in (periodic: the face at the last cell pairs
 // with the first cell; mirror: the ghost-side state is the signed copy of
 // the interior one).
-template <int DIR>
+// With a tape (tlim, tface non-null) the limiter selections and the HLLD
+// branches are the recorded ones, else they are recomputed from W.
+template <int DIR, int MODE>
 __device__ __forceinline__ void face_vjp(const AdjGeo& g, const double* __restrict__ W, const double* __restrict__ lam,
-                                         double gscale, double ch, int q, int f, double* __restrict__ gUp,
+                                         double gscale, double ch, int q, int f, const unsigned char* __restrict__ tlim,
+                                         const unsigned short* __restrict__ tface, double* __restrict__ gUp,
                                          double* __restrict__ gLo) {
   constexpr int A = DIR - 1;
   const int nx = (DIR == 1) ? g.ix : g.jx;
@@ -145,12 +153,14 @@ __device__ __forceinline__ void face_vjp(const AdjGeo& g, const double* __restri
   const bool lo_wall = (f == 0);
   const int mr = (f == nx - 2) ? (per ? 1 : -1) : f + 1;  // cell whose lower state is R
   double L[NV], R[NV];
+  const unsigned char* tl = (MODE == tape::kReplay) ? tlim + (size_t)A * NV * n : nullptr;
   if (!lo_wall) {
     const size_t c0 = base + (size_t)f * s;
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       double up, lo;
-      reconstruct_fp64<true>(g.lm, W[v * n + c0 - s], W[v * n + c0], W[v * n + c0 + s], up, lo);
+      unsigned char k = (MODE == tape::kReplay) ? tl[v * n + c0] : 0;
+      reconstruct_fp64<true, MODE>(g.lm, W[v * n + c0 - s], W[v * n + c0], W[v * n + c0 + s], up, lo, &k);
       L[v] = up;
     }
   }
@@ -159,7 +169,8 @@ __device__ __forceinline__ void face_vjp(const AdjGeo& g, const double* __restri
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       double up, lo;
-      reconstruct_fp64<true>(g.lm, W[v * n + c0 - s], W[v * n + c0], W[v * n + c0 + s], up, lo);
+      unsigned char k = (MODE == tape::kReplay) ? tl[v * n + c0] : 0;
+      reconstruct_fp64<true, MODE>(g.lm, W[v * n + c0 - s], W[v * n + c0], W[v * n + c0 + s], up, lo, &k);
       R[v] = lo;
     }
   }
@@ -179,7 +190,8 @@ __device__ __forceinline__ void face_vjp(const AdjGeo& g, const double* __restri
     gF[v] = gscale * (lr - ll);
   }
   double gL[NV], gR[NV];
-  adj::hlld_vjp<DIR>(L, R, ch, g.gamma, gF, gL, gR);
+  unsigned hk = (MODE == tape::kReplay) ? tface[(size_t)A * n + base + (size_t)f * s] : 0u;
+  adj::hlld_vjp<DIR, MODE>(L, R, ch, g.gamma, gF, gL, gR, &hk);
   const size_t up_off = (size_t)A * NV * n, lo_off = up_off;
   if (lo_wall) {
     const size_t c1 = base + s;
@@ -204,21 +216,23 @@ __device__ __forceinline__ void face_vjp(const AdjGeo& g, const double* __restri
 // x faces (rows 1..jx-2, faces 0..ix-2) in the first nbx blocks, y faces
 // (columns 1..ix-2, faces 0..jx-2) in the rest; consecutive threads take
 // consecutive cells along x in both.
+template <int MODE>
 __global__ void __launch_bounds__(128) k_adj_faces(AdjGeo g, const double* __restrict__ W,
                                                    const double* __restrict__ lam, const double* __restrict__ lg,
-                                                   double lscale, int nbx, double* __restrict__ gUp,
-                                                   double* __restrict__ gLo) {
+                                                   double lscale, int nbx, const unsigned char* __restrict__ tlim,
+                                                   const unsigned short* __restrict__ tface,
+                                                   double* __restrict__ gUp, double* __restrict__ gLo) {
   const double dt = lg[0], ch = lg[1];
   if ((int)blockIdx.x < nbx) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int nf = g.ix - 1;
     if (t >= (long long)nf * (g.jx - 2)) return;
-    face_vjp<1>(g, W, lam, lscale * (dt / g.dx), ch, 1 + (int)(t / nf), (int)(t % nf), gUp, gLo);
+    face_vjp<1, MODE>(g, W, lam, lscale * (dt / g.dx), ch, 1 + (int)(t / nf), (int)(t % nf), tlim, tface, gUp, gLo);
   } else {
     const long long t = (long long)(blockIdx.x - nbx) * blockDim.x + threadIdx.x;
     const int nq = g.ix - 2;
     if (t >= (long long)nq * (g.jx - 1)) return;
-    face_vjp<2>(g, W, lam, lscale * (dt / g.dy), ch, 1 + (int)(t % nq), (int)(t / nq), gUp, gLo);
+    face_vjp<2, MODE>(g, W, lam, lscale * (dt / g.dy), ch, 1 + (int)(t % nq), (int)(t / nq), tlim, tface, gUp, gLo);
   }
 }
 
@@ -230,6 +244,7 @@ __global__ void __launch_bounds__(256) k_adj_cells(AdjGeo g, const double* __res
                                                    const double* __restrict__ gLo, const double* __restrict__ Ain,
                                                    double a1, const double* __restrict__ Bin,
                                                    const double* __restrict__ lg, int out_glm,
+                                                   const unsigned char* __restrict__ tlim,
                                                    double* __restrict__ out) {
   const size_t n = g.n;
   const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -254,8 +269,9 @@ __global__ void __launch_bounds__(256) k_adj_cells(AdjGeo g, const double* __res
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
         double gm = 0.0, g0 = 0.0, gp = 0.0;
-        adj::recon_vjp(g.lm, W[v * n + cm - s], W[v * n + cm], W[v * n + cm + s], gUp[(A * NV + v) * n + cm],
-                       gLo[(A * NV + v) * n + cm], gm, g0, gp);
+        const unsigned char k = tlim ? tlim[(A * NV + v) * n + cm]
+                                     : adj::recon_code(g.lm, W[v * n + cm - s], W[v * n + cm], W[v * n + cm + s]);
+        adj::recon_vjp_code(g.lm, k, gUp[(A * NV + v) * n + cm], gLo[(A * NV + v) * n + cm], gm, g0, gp);
         gw[v] += (d == -1) ? gm : ((d == 0) ? g0 : gp);
       }
     }
@@ -298,6 +314,13 @@ __global__ void k_log_step(const StepState* __restrict__ st, double* __restrict_
   out[2] = st->glm_f;
 }
 
+// the step about to run takes a recorded {dt, ch, glm factor}
+__global__ void k_force_step(StepState* __restrict__ st, const double* __restrict__ in) {
+  st->dt = in[0];
+  st->ch = in[1];
+  st->glm_f = in[2];
+}
+
 }  // namespace
 }  // namespace omhd
 
@@ -314,6 +337,10 @@ struct omhd_adjoint {
   StepState* ckst = nullptr; // nck step records
   double* segU = nullptr;    // every states U^k of the segment being reversed
   double* segU1 = nullptr;   // every stage-1 results U1^k
+  unsigned char* segTl = nullptr;   // decision tape of the segment: every x 2 stages
+  unsigned short* segTf = nullptr;
+  unsigned char* fullTl = nullptr;  // decision tape of a whole recorded run (nsteps x 2 stages)
+  unsigned short* fullTf = nullptr;
   double* Uw = nullptr;      // working state of the forward runs
   double* U1w = nullptr;     // stage buffer of the plain forward run
   double* logd = nullptr;    // 3 * nsteps
@@ -322,7 +349,7 @@ struct omhd_adjoint {
   double* gLo = nullptr;     // 2 * NV planes
   double* lam[3] = {nullptr, nullptr, nullptr};
   size_t bytes = 0;
-  bool have_forward = false;
+  bool have_forward = false, have_tape = false;
   omhd_error_info last = {};
 };
 
@@ -337,28 +364,58 @@ int acerr(omhd_adjoint* a, cudaError_t e, const char* where) {
   return OMHD_CUDA_ERR;
 }
 
-int amalloc(omhd_adjoint* a, double** p, size_t doubles, const char* what) {
-  const int r = acerr(a, cudaMalloc(p, sizeof(double) * doubles), what);
-  if (!r) a->bytes += sizeof(double) * doubles;
+template <class P>
+int amalloc(omhd_adjoint* a, P** p, size_t count, const char* what) {
+  const int r = acerr(a, cudaMalloc(p, sizeof(P) * count), what);
+  if (!r) a->bytes += sizeof(P) * count;
   return r;
 }
 
+// decision-tape slots of one stage
+size_t tl_stride(const omhd_adjoint* a) { return (size_t)2 * NV * a->n; }
+size_t tf_stride(const omhd_adjoint* a) { return (size_t)2 * a->n; }
+
+// One fused step of the solver's bound state with its stages' decisions
+// recorded in (or replayed from) the tape slots tl[0..1], tf[0..1].
+int taped_step(omhd_adjoint* a, int mode, unsigned char* tl, unsigned short* tf) {
+  for (int stage = 1; stage <= 2; ++stage) {
+    StageArgs sa = make_stage_args(a->s, stage);
+    sa.tlim = tl + (size_t)(stage - 1) * tl_stride(a);
+    sa.tface = tf + (size_t)(stage - 1) * tf_stride(a);
+    const int e = launch_stage2d_fp64_tape(sa, mode, a->stream);
+    if (e) return acerr(a, (cudaError_t)e, "taped stage kernel launch");
+  }
+  return OMHD_OK;
+}
+
 int launch_step_vjp(omhd_adjoint* a, const double* Un, const double* U1, const double* lg, double* lam_in,
-                    double* lam1, double* lam_out) {
+                    double* lam1, double* lam_out, const unsigned char* tl, const unsigned short* tf) {
   const AdjGeo& g = a->geo;
   const int TPB = 256, FPB = 128;
   const int cb = ceil_div((long long)g.n, TPB);
   const int nbx = ceil_div((long long)(g.ix - 1) * (g.jx - 2), FPB);
   const int nby = ceil_div((long long)(g.ix - 2) * (g.jx - 1), FPB);
   cudaStream_t st = a->stream;
+  const unsigned char* tl1 = tl;
+  const unsigned char* tl2 = tl ? tl + tl_stride(a) : nullptr;
+  const unsigned short* tf1 = tf;
+  const unsigned short* tf2 = tf ? tf + tf_stride(a) : nullptr;
   // stage 2: U' = 0.5 (Ua + U1 + D(U1)), then bc and the second GLM half
   k_adj_prim<<<cb, TPB, 0, st>>>(g, U1, lg, 0, a->W, lam_in, 1);
-  k_adj_faces<<<nbx + nby, FPB, 0, st>>>(g, a->W, lam_in, lg, 0.5, nbx, a->gUp, a->gLo);
-  k_adj_cells<<<cb, TPB, 0, st>>>(g, U1, a->W, a->gUp, a->gLo, lam_in, 0.5, nullptr, lg, 0, lam1);
+  if (tl)
+    k_adj_faces<tape::kReplay><<<nbx + nby, FPB, 0, st>>>(g, a->W, lam_in, lg, 0.5, nbx, tl2, tf2, a->gUp, a->gLo);
+  else
+    k_adj_faces<tape::kNone><<<nbx + nby, FPB, 0, st>>>(g, a->W, lam_in, lg, 0.5, nbx, nullptr, nullptr, a->gUp,
+                                                         a->gLo);
+  k_adj_cells<<<cb, TPB, 0, st>>>(g, U1, a->W, a->gUp, a->gLo, lam_in, 0.5, nullptr, lg, 0, tl2, lam1);
   // stage 1: U1 = bc(Ua + D(Ua)), Ua = first GLM half of U^n
   k_adj_prim<<<cb, TPB, 0, st>>>(g, Un, lg, 1, a->W, lam1, 0);
-  k_adj_faces<<<nbx + nby, FPB, 0, st>>>(g, a->W, lam1, lg, 1.0, nbx, a->gUp, a->gLo);
-  k_adj_cells<<<cb, TPB, 0, st>>>(g, Un, a->W, a->gUp, a->gLo, lam_in, 0.5, lam1, lg, 1, lam_out);
+  if (tl)
+    k_adj_faces<tape::kReplay><<<nbx + nby, FPB, 0, st>>>(g, a->W, lam1, lg, 1.0, nbx, tl1, tf1, a->gUp, a->gLo);
+  else
+    k_adj_faces<tape::kNone><<<nbx + nby, FPB, 0, st>>>(g, a->W, lam1, lg, 1.0, nbx, nullptr, nullptr, a->gUp,
+                                                         a->gLo);
+  k_adj_cells<<<cb, TPB, 0, st>>>(g, Un, a->W, a->gUp, a->gLo, lam_in, 0.5, lam1, lg, 1, tl1, lam_out);
   return acerr(a, cudaGetLastError(), "adjoint step kernels");
 }
 
@@ -370,6 +427,41 @@ int validate_adjoint(const omhd_config* c) {
   if (c->time_type != OMHD_TIME_TVDRK2) return OMHD_NOT_SUPPORTED;
   if (c->eta_kind != OMHD_ETA_NONE) return OMHD_NOT_SUPPORTED;
   return OMHD_OK;
+}
+
+// Forward run from U0 (copied, bc applied): checkpoints and the step log,
+// optionally the full decision tape (mode tape::kRecord) or, with
+// tape::kReplay, every decision and every {dt, ch, glm factor} taken from a
+// recorded run.
+int run_forward(omhd_adjoint* a, const double* U0, double* UN, int mode) {
+  omhd_solver* s = a->s;
+  const size_t S = NV * a->n;
+  int r = omhd_solver_bind(s, a->Uw, a->U1w);
+  r = r ? r : omhd_solver_put_state(s, U0, 0.0);  // copy, bc, plan the first dt
+  for (int k = 0; k < a->nsteps && !r; ++k) {
+    if (mode != tape::kReplay && k % a->every == 0) {
+      const int q = k / a->every;
+      r = acerr(a, cudaMemcpyAsync(a->ck + S * q, a->Uw, sizeof(double) * S, cudaMemcpyDeviceToDevice, a->stream),
+                "checkpoint copy");
+      r = r ? r
+            : acerr(a, cudaMemcpyAsync(a->ckst + q, s->st, sizeof(StepState), cudaMemcpyDeviceToDevice, a->stream),
+                    "checkpoint record copy");
+    }
+    if (r) break;
+    if (mode == tape::kReplay)
+      k_force_step<<<1, 1, 0, a->stream>>>(s->st, a->logd + 3 * (size_t)k);
+    else
+      k_log_step<<<1, 1, 0, a->stream>>>(s->st, a->logd + 3 * (size_t)k);
+    r = acerr(a, cudaGetLastError(), "step record kernel");
+    if (r) break;
+    if (mode == tape::kNone)
+      r = omhd_solver_step(s, 1);
+    else
+      r = taped_step(a, mode, a->fullTl + 2 * tl_stride(a) * k, a->fullTf + 2 * tf_stride(a) * k);
+  }
+  if (!r && UN)
+    r = acerr(a, cudaMemcpyAsync(UN, a->Uw, sizeof(double) * S, cudaMemcpyDeviceToDevice, a->stream), "state copy");
+  return r;
 }
 
 }  // namespace
@@ -411,6 +503,8 @@ int omhd_adjoint_create(const omhd_config* cfg, int nsteps, int checkpoint_every
   r = r ? r : amalloc(a, &a->ck, S * a->nck, "checkpoint allocation");
   r = r ? r : amalloc(a, &a->segU, S * a->every, "segment allocation");
   r = r ? r : amalloc(a, &a->segU1, S * a->every, "segment allocation");
+  r = r ? r : amalloc(a, &a->segTl, 2 * tl_stride(a) * a->every, "segment tape allocation");
+  r = r ? r : amalloc(a, &a->segTf, 2 * tf_stride(a) * a->every, "segment tape allocation");
   r = r ? r : amalloc(a, &a->Uw, S, "work state allocation");
   r = r ? r : amalloc(a, &a->U1w, S, "work state allocation");
   r = r ? r : amalloc(a, &a->logd, 3 * (size_t)nsteps, "step log allocation");
@@ -418,9 +512,10 @@ int omhd_adjoint_create(const omhd_config* cfg, int nsteps, int checkpoint_every
   r = r ? r : amalloc(a, &a->gUp, 2 * S, "adjoint work allocation");
   r = r ? r : amalloc(a, &a->gLo, 2 * S, "adjoint work allocation");
   for (int q = 0; q < 3; ++q) r = r ? r : amalloc(a, &a->lam[q], S, "adjoint work allocation");
-  if (!r) {
-    r = acerr(a, cudaMalloc(&a->ckst, sizeof(StepState) * a->nck), "checkpoint record allocation");
-    if (!r) a->bytes += sizeof(StepState) * a->nck;
+  r = r ? r : amalloc(a, &a->ckst, (size_t)a->nck, "checkpoint record allocation");
+  if (!r) {  // tape entries of cells no stage records (ghosts) stay defined
+    r = acerr(a, cudaMemset(a->segTl, 0, 2 * tl_stride(a) * a->every), "tape clear");
+    r = r ? r : acerr(a, cudaMemset(a->segTf, 0, sizeof(unsigned short) * 2 * tf_stride(a) * a->every), "tape clear");
   }
   if (!r) r = omhd_solver_bind(a->s, a->Uw, a->U1w);
   if (r) {
@@ -434,11 +529,10 @@ int omhd_adjoint_create(const omhd_config* cfg, int nsteps, int checkpoint_every
 int omhd_adjoint_destroy(omhd_adjoint* a) {
   if (!a) return OMHD_OK;
   if (a->s) omhd_solver_destroy(a->s);
-  double* bufs[] = {a->ck, a->segU, a->segU1, a->Uw, a->U1w, a->logd, a->W, a->gUp, a->gLo,
-                    a->lam[0], a->lam[1], a->lam[2]};
-  for (double* p : bufs)
+  void* bufs[] = {a->ck,   a->segU, a->segU1, a->segTl,  a->segTf,  a->fullTl, a->fullTf, a->Uw, a->U1w,
+                  a->logd, a->W,    a->gUp,   a->gLo,    a->lam[0], a->lam[1], a->lam[2], a->ckst};
+  for (void* p : bufs)
     if (p) cudaFree(p);
-  if (a->ckst) cudaFree(a->ckst);
   delete a;
   return OMHD_OK;
 }
@@ -451,36 +545,40 @@ int omhd_adjoint_set_stream(omhd_adjoint* a, void* stream) {
 
 int omhd_adjoint_forward(omhd_adjoint* a, const double* U0, double* UN) {
   if (!a || !U0) return OMHD_BAD_ARG;
-  omhd_solver* s = a->s;
-  const size_t S = NV * a->n;
   a->have_forward = false;
-  int r = omhd_solver_bind(s, a->Uw, a->U1w);
-  r = r ? r : omhd_solver_put_state(s, U0, 0.0);  // copy, bc, plan the first dt
-  for (int k = 0; k < a->nsteps && !r; ++k) {
-    if (k % a->every == 0) {
-      const int q = k / a->every;
-      r = acerr(a, cudaMemcpyAsync(a->ck + S * q, a->Uw, sizeof(double) * S, cudaMemcpyDeviceToDevice, a->stream),
-                "checkpoint copy");
-      r = r ? r
-            : acerr(a, cudaMemcpyAsync(a->ckst + q, s->st, sizeof(StepState), cudaMemcpyDeviceToDevice, a->stream),
-                    "checkpoint record copy");
-    }
-    if (!r) {
-      k_log_step<<<1, 1, 0, a->stream>>>(s->st, a->logd + 3 * (size_t)k);
-      r = acerr(a, cudaGetLastError(), "step log kernel");
-    }
-    r = r ? r : omhd_solver_step(s, 1);
-  }
-  if (!r && UN)
-    r = acerr(a, cudaMemcpyAsync(UN, a->Uw, sizeof(double) * S, cudaMemcpyDeviceToDevice, a->stream), "state copy");
+  const int r = run_forward(a, U0, UN, tape::kNone);
   if (!r) a->have_forward = true;
   return r;
+}
+
+int omhd_adjoint_record(omhd_adjoint* a, const double* U0, double* UN) {
+  if (!a || !U0) return OMHD_BAD_ARG;
+  int r = OMHD_OK;
+  if (!a->fullTl) {
+    r = amalloc(a, &a->fullTl, 2 * tl_stride(a) * a->nsteps, "tape allocation");
+    r = r ? r : amalloc(a, &a->fullTf, 2 * tf_stride(a) * a->nsteps, "tape allocation");
+    r = r ? r : acerr(a, cudaMemsetAsync(a->fullTl, 0, 2 * tl_stride(a) * a->nsteps, a->stream), "tape clear");
+    r = r ? r
+          : acerr(a, cudaMemsetAsync(a->fullTf, 0, sizeof(unsigned short) * 2 * tf_stride(a) * a->nsteps, a->stream),
+                  "tape clear");
+    if (r) return r;
+  }
+  a->have_forward = a->have_tape = false;
+  r = run_forward(a, U0, UN, tape::kRecord);
+  if (!r) a->have_forward = a->have_tape = true;
+  return r;
+}
+
+int omhd_adjoint_replay(omhd_adjoint* a, const double* U0, double* UN) {
+  if (!a || !U0) return OMHD_BAD_ARG;
+  if (!a->have_tape) return OMHD_BAD_ARG;
+  return run_forward(a, U0, UN, tape::kReplay);
 }
 
 int omhd_adjoint_step_vjp(omhd_adjoint* a, const double* Un, const double* U1, const double* log3, double* lam_in,
                           double* lam_out) {
   if (!a || !Un || !U1 || !log3 || !lam_in || !lam_out || lam_in == lam_out) return OMHD_BAD_ARG;
-  return launch_step_vjp(a, Un, U1, log3, lam_in, a->lam[2], lam_out);
+  return launch_step_vjp(a, Un, U1, log3, lam_in, a->lam[2], lam_out, nullptr, nullptr);
 }
 
 int omhd_adjoint_backward(omhd_adjoint* a, const double* gUN, double* gU0) {
@@ -494,21 +592,24 @@ int omhd_adjoint_backward(omhd_adjoint* a, const double* gUN, double* gU0) {
   for (int q = a->nck - 1; q >= 0 && !r; --q) {
     const int k0 = q * a->every;
     const int k1 = (k0 + a->every < a->nsteps) ? k0 + a->every : a->nsteps;
-    // recompute the segment from its checkpoint, keeping each step's stage inputs
+    // recompute the segment from its checkpoint, keeping each step's stage
+    // inputs and recording its decisions
     r = acerr(a, cudaMemcpyAsync(a->Uw, a->ck + S * q, sizeof(double) * S, cudaMemcpyDeviceToDevice, a->stream),
               "checkpoint restore");
     r = r ? r : acerr(a, cudaMemcpyAsync(s->st, a->ckst + q, sizeof(StepState), cudaMemcpyDeviceToDevice, a->stream),
                       "checkpoint record restore");
     for (int k = k0; k < k1 && !r; ++k) {
-      double* Uk = a->segU + S * (k - k0);
+      const int j = k - k0;
+      double* Uk = a->segU + S * j;
       r = acerr(a, cudaMemcpyAsync(Uk, a->Uw, sizeof(double) * S, cudaMemcpyDeviceToDevice, a->stream), "segment copy");
-      r = r ? r : omhd_solver_bind(s, a->Uw, a->segU1 + S * (k - k0));
-      r = r ? r : omhd_solver_step(s, 1);
+      r = r ? r : omhd_solver_bind(s, a->Uw, a->segU1 + S * j);
+      r = r ? r : taped_step(a, tape::kRecord, a->segTl + 2 * tl_stride(a) * j, a->segTf + 2 * tf_stride(a) * j);
     }
     // reverse the segment
     for (int k = k1 - 1; k >= k0 && !r; --k) {
-      r = launch_step_vjp(a, a->segU + S * (k - k0), a->segU1 + S * (k - k0), a->logd + 3 * (size_t)k, lcur,
-                          a->lam[2], lnext);
+      const int j = k - k0;
+      r = launch_step_vjp(a, a->segU + S * j, a->segU1 + S * j, a->logd + 3 * (size_t)k, lcur, a->lam[2], lnext,
+                          a->segTl + 2 * tl_stride(a) * j, a->segTf + 2 * tf_stride(a) * j);
       double* t = lcur;
       lcur = lnext;
       lnext = t;

@@ -12,6 +12,9 @@
 #pragma once
 #include <cmath>
 
+#include "omhd_fastmath.h"
+#include "omhd_tape.h"
+
 #ifdef __CUDACC__
 #define OMHD_HD __host__ __device__ __forceinline__
 #else
@@ -21,12 +24,31 @@
 namespace omhd {
 namespace adj {
 
+// 1/x and 1/sqrt(x): Newton-Raphson from the hardware approximations on the
+// device (omhd_fastmath.h, ~1 ulp), IEEE on the host.  Every denominator is
+// inverted once and its uses multiply.
+OMHD_HD double arcp(double x) {
+#ifdef __CUDA_ARCH__
+  return rcp_nr(x);
+#else
+  return 1.0 / x;
+#endif
+}
+OMHD_HD double arsqrt(double x) {
+#ifdef __CUDA_ARCH__
+  return rsqrt_nr(x);
+#else
+  return 1.0 / std::sqrt(x);
+#endif
+}
+
 // slots: w = (vx vy vz p rho Bx By Bz psi); U/F = (mx my mz E rho Bx By Bz psi)
 constexpr int kVX = 0, kPR = 3, kRO = 4, kBX = 5, kPS = 8, kEN = 3;
 
 struct Side {
-  double v2, B2, vB, Um[3], UE, F[9], f1, f2, Q, D, sq, a, pt;
+  double v2, B2, vB, Um[3], UE, F[9], f1, f2, Q, D, sq, a, pt, ir, isq;
 };
+using tape::decide;
 struct SideG {
   double Um[3], UE, F[9], a, pt, vB;
 };
@@ -39,8 +61,9 @@ OMHD_HD void zero(SideG& g) {
 
 // one side of the face: conserved state, physical flux, fast-speed^2 proxy,
 // total pressure (flux_solver.f90:359-379)
-template <int DIR>
-OMHD_HD void side_fwd(const double* s, double gamma, double r1, double r2, Side& o) {
+template <int DIR, int MODE = tape::kNone>
+OMHD_HD void side_fwd(const double* s, double gamma, double r1, double r2, Side& o, unsigned* code = nullptr,
+                      unsigned clamp_bit = 0) {
   constexpr int vn = (DIR - 1) % 3, vt1 = DIR % 3, vt2 = (DIR + 1) % 3;
   constexpr int bn = kBX + (DIR - 1) % 3, bt1 = kBX + DIR % 3, bt2 = kBX + (DIR + 1) % 3;
   constexpr int mn = vn, mt1 = vt1, mt2 = vt2;
@@ -61,8 +84,11 @@ OMHD_HD void side_fwd(const double* s, double gamma, double r1, double r2, Side&
   o.f2 = 4 * (s[bn] * s[bn]);
   o.Q = o.f1 + o.B2;
   o.D = o.Q * o.Q - o.f1 * o.f2;
-  o.sq = std::sqrt((0.0 > o.D) ? 0.0 : o.D);
-  o.a = (o.Q + o.sq) / (2 * s[kRO]);
+  const double Dc = decide<MODE>(0.0 > o.D, code, clamp_bit) ? 0.0 : o.D;  // fmax2(D, 0)
+  o.isq = (Dc > 0.0) ? arsqrt(Dc) : 0.0;
+  o.sq = Dc * o.isq;
+  o.ir = arcp(s[kRO]);
+  o.a = (o.Q + o.sq) * (0.5 * o.ir);
   o.pt = s[kPR] + 0.5 * o.B2;
 }
 
@@ -78,11 +104,11 @@ OMHD_HD void side_adj(const double* s, double gamma, double r1, double r2, const
   gp += g.pt;
   gB2 += 0.5 * g.pt;
   // a = (Q + sq) / (2 rho)
-  const double gnum = g.a / (2 * s[kRO]);
-  gro -= g.a * o.a / s[kRO];
+  const double gnum = g.a * (0.5 * o.ir);
+  gro -= g.a * o.a * o.ir;
   double gQ = gnum;
   const double gsq = gnum;
-  const double gD = (o.D > 0.0 && o.sq > 0.0) ? gsq * 0.5 / o.sq : 0.0;
+  const double gD = (o.D > 0.0) ? gsq * 0.5 * o.isq : 0.0;
   gQ += 2 * o.Q * gD;
   double gf1 = -o.f2 * gD;
   const double gf2 = -o.f1 * gD;
@@ -169,13 +195,16 @@ OMHD_HD void side_adj(const double* s, double gamma, double r1, double r2, const
 }
 
 // gL, gR = (dF/dL)^T gF, (dF/dR)^T gF for the HLLD flux F(L, R) with ch fixed.
-template <int DIR>
+// MODE tape::kReplay takes every branch and selection from *code (the
+// forward's decision tape, omhd_tape.h); otherwise they are recomputed from
+// L and R (and recorded in *code under tape::kRecord).
+template <int DIR, int MODE = tape::kNone>
 OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma, const double* gF, double* gL,
-                      double* gR) {
+                      double* gR, unsigned* code = nullptr) {
   constexpr int vn = (DIR - 1) % 3, vt1 = DIR % 3, vt2 = (DIR + 1) % 3;
   constexpr int bn = kBX + (DIR - 1) % 3, bt1 = kBX + DIR % 3, bt2 = kBX + (DIR + 1) % 3;
   constexpr int mn = vn, mt1 = vt1, mt2 = vt2;
-  const double r1 = 1.0 / (gamma - 1.0), r2 = gamma / (gamma - 1.0);
+  const double r1 = arcp(gamma - 1.0), r2 = gamma * r1;
   const double hf = 1.001;
   for (int k = 0; k < 9; ++k) {
     gL[k] = 0.0;
@@ -188,28 +217,29 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
   gR[bn] += -0.5 * ch * gF[bn] + 0.5 * (ch * ch) * gF[kPS];
 
   Side sL, sR;
-  side_fwd<DIR>(L, gamma, r1, r2, sL);
-  side_fwd<DIR>(R, gamma, r1, r2, sR);
+  side_fwd<DIR, MODE>(L, gamma, r1, r2, sL, code, tape::kClampL);
+  side_fwd<DIR, MODE>(R, gamma, r1, r2, sR, code, tape::kClampR);
   SideG gsL, gsR;
   zero(gsL);
   zero(gsR);
   const int fl[7] = {kRO, mn, mt1, mt2, kEN, bt1, bt2};  // slots set from the physical fluxes
 
-  const bool aRsel = sR.a > sL.a;  // fmax2(aL, aR)
+  const bool aRsel = decide<MODE>(sR.a > sL.a, code, tape::kArSel);  // fmax2(aL, aR)
   const double amax = aRsel ? sR.a : sL.a;
-  const double cf = std::sqrt(amax);
-  const bool minR = R[vn] < L[vn];  // fmin2(vnL, vnR)
-  const bool maxR = R[vn] > L[vn];  // fmax2(vnL, vnR)
+  const double icf = (amax > 0.0) ? arsqrt(amax) : 0.0;
+  const double cf = amax * icf;
+  const bool minR = decide<MODE>(R[vn] < L[vn], code, tape::kMinR);  // fmin2(vnL, vnR)
+  const bool maxR = decide<MODE>(R[vn] > L[vn], code, tape::kMaxR);  // fmax2(vnL, vnR)
   const double SL = (minR ? R[vn] : L[vn]) - cf;
   const double SR = (maxR ? R[vn] : L[vn]) + cf;
   double gSL = 0.0, gSR = 0.0;
 
-  if (SL >= 0.0) {
+  if (decide<MODE>(SL >= 0.0, code, tape::kFL)) {
     for (int q = 0; q < 7; ++q) gsL.F[fl[q]] += gF[fl[q]];
-  } else if (SR <= 0.0) {
+  } else if (decide<MODE>(SR <= 0.0, code, tape::kFR)) {
     for (int q = 0; q < 7; ++q) gsR.F[fl[q]] += gF[fl[q]];
   } else {
-    const double ih = 1.0 / (SR - SL);
+    const double ih = arcp(SR - SL);
     double NU[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, Uh[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int k = 0; k < 3; ++k) {
       NU[k] = SR * sR.Um[k] - SL * sL.Um[k] - sR.F[k] + sL.F[k];
@@ -219,21 +249,25 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
       NU[k] = SR * R[k] - SL * L[k] - sR.F[k] + sL.F[k];
       Uh[k] = ih * NU[k];
     }
-    const double aM = Uh[mn] / Uh[kRO];
+    const double iUr = arcp(Uh[kRO]);
+    const double aM = Uh[mn] * iUr;
     const double tL = SL - L[vn], tR = SR - R[vn];
     const double pts = sL.pt + L[kRO] * tL * (aM - L[vn]);
     const double eL = SL - aM, eR = SR - aM;
-    const double roL = L[kRO] * tL / eL, roR = R[kRO] * tR / eR;
+    const double ieL = arcp(eL), ieR = arcp(eR);
+    const double roL = L[kRO] * tL * ieL, roR = R[kRO] * tR * ieR;
     const double Ubn = Uh[bn];
-    const double aUbn = std::fabs(Ubn);
-    const double sqL = std::sqrt(roL), sqR = std::sqrt(roR);
-    const double aVL = aUbn / sqL, aVR = aUbn / sqR;
+    const bool bneg = decide<MODE>(std::signbit(Ubn), code, tape::kBnNeg);
+    const double aUbn = (MODE == tape::kNone) ? std::fabs(Ubn) : (bneg ? -Ubn : Ubn);
+    const double isqL = arsqrt(roL), isqR = arsqrt(roR);
+    const double sqL = roL * isqL, sqR = roR * isqR;
+    const double aVL = aUbn * isqL, aVR = aUbn * isqR;
 
     double gUh[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     double gih = 0.0, gaM = 0.0, gpts = 0.0, gtL = 0.0, gtR = 0.0, geL = 0.0, geR = 0.0;
     double groL = 0.0, groR = 0.0, gaVL = 0.0, gaVR = 0.0, gsqL = 0.0, gsqR = 0.0;
 
-    if ((SL >= (aM - hf * aVL)) || ((aM + hf * aVR) >= SR)) {
+    if (decide<MODE>((SL >= (aM - hf * aVL)) || ((aM + hf * aVR) >= SR), code, tape::kG)) {
       // ---- HLLC-G fallback (flux_solver.f90:450-476) ----
       const double f2g = SL * SR;
       double gf2g = 0.0;
@@ -253,18 +287,18 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
       }
       gSL += gf2g * SR;
       gSR += gf2g * SL;
-      const double at1 = Uh[mt1] / Uh[kRO], at2 = Uh[mt2] / Uh[kRO];
+      const double at1 = Uh[mt1] * iUr, at2 = Uh[mt2] * iUr;
       double gat1 = 0.0, gat2 = 0.0;
-      const bool left = !std::signbit(aM);  // 0.5 + sign(0.5, aM) == 1
+      const bool left = decide<MODE>(!std::signbit(aM), code, tape::kGLeft);  // 0.5 + sign(0.5, aM) == 1
       const double* S = left ? L : R;
       const Side& sS = left ? sL : sR;
       SideG& gsS = left ? gsL : gsR;
       double* gS = left ? gL : gR;
       const double Sw = left ? SL : SR;
-      const double tS = left ? tL : tR, eS = left ? eL : eR, roS = left ? roL : roR;
+      const double tS = left ? tL : tR, ieS = left ? ieL : ieR, roS = left ? roL : roR;
       const double QS = sS.vB - aM * Ubn - at1 * Uh[bt1] - at2 * Uh[bt2];
       const double numS = tS * sS.UE - sS.pt * S[vn] + pts * aM + Ubn * QS;
-      const double enS = numS / eS;
+      const double enS = numS * ieS;
       double gSw = gF[mn] * (roS * aM - sS.Um[mn]) + gF[mt1] * (roS * at1 - sS.Um[mt1]) +
                    gF[mt2] * (roS * at2 - sS.Um[mt2]) + gF[kEN] * (enS - sS.UE) + gF[kRO] * (roS - S[kRO]);
       const double groS = Sw * (gF[mn] * aM + gF[mt1] * at1 + gF[mt2] * at2 + gF[kRO]);
@@ -283,8 +317,8 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
       gsS.F[kEN] += gF[kEN];
       gsS.F[kRO] += gF[kRO];
       // en = num / e
-      const double gnum = genS / eS;
-      double geS = -genS * enS / eS, gtS = 0.0;
+      const double gnum = genS * ieS;
+      double geS = -genS * enS * ieS, gtS = 0.0;
       gtS += gnum * sS.UE;
       gsS.UE += gnum * tS;
       gsS.pt -= gnum * S[vn];
@@ -300,10 +334,10 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
       gUh[bt1] -= gQ * at1;
       gat2 -= gQ * Uh[bt2];
       gUh[bt2] -= gQ * at2;
-      gUh[mt1] += gat1 / Uh[kRO];
-      gUh[kRO] -= gat1 * at1 / Uh[kRO];
-      gUh[mt2] += gat2 / Uh[kRO];
-      gUh[kRO] -= gat2 * at2 / Uh[kRO];
+      gUh[mt1] += gat1 * iUr;
+      gUh[kRO] -= gat1 * at1 * iUr;
+      gUh[mt2] += gat2 * iUr;
+      gUh[kRO] -= gat2 * at2 * iUr;
       if (left) {
         gSL += gSw;
         groL += groS;
@@ -318,26 +352,26 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
     } else {
       // ---- HLLD (flux_solver.f90:482-572) ----
       // L* and R* intermediate states
-      const double dL = L[kRO] * tL * eL - Ubn * Ubn, iL = 1.0 / dL;
+      const double dL = L[kRO] * tL * eL - Ubn * Ubn, iL = arcp(dL);
       const double kL = L[kRO] * (tL * tL) - Ubn * Ubn;
       const double UL1bt1 = L[bt1] * iL * kL, UL1bt2 = L[bt2] * iL * kL;
       const double dmL = aM - L[vn];
       const double vt1L = L[vt1] - iL * Ubn * L[bt1] * dmL, vt2L = L[vt2] - iL * Ubn * L[bt2] * dmL;
       const double QL = sL.vB - aM * Ubn - vt1L * UL1bt1 - vt2L * UL1bt2;
       const double numL = tL * sL.UE - sL.pt * L[vn] + pts * aM + Ubn * QL;
-      const double UL1E = numL / eL;
+      const double UL1E = numL * ieL;
       double UL1m[3];
       UL1m[mn] = roL * aM;
       UL1m[mt1] = roL * vt1L;
       UL1m[mt2] = roL * vt2L;
-      const double dR = R[kRO] * tR * eR - Ubn * Ubn, iR = 1.0 / dR;
+      const double dR = R[kRO] * tR * eR - Ubn * Ubn, iR = arcp(dR);
       const double kR = R[kRO] * (tR * tR) - Ubn * Ubn;
       const double UR1bt1 = R[bt1] * iR * kR, UR1bt2 = R[bt2] * iR * kR;
       const double dmR = aM - R[vn];
       const double vt1R = R[vt1] - iR * Ubn * R[bt1] * dmR, vt2R = R[vt2] - iR * Ubn * R[bt2] * dmR;
       const double QR = sR.vB - aM * Ubn - vt1R * UR1bt1 - vt2R * UR1bt2;
       const double numR = tR * sR.UE - sR.pt * R[vn] + pts * aM + Ubn * QR;
-      const double UR1E = numR / eR;
+      const double UR1E = numR * ieR;
       double UR1m[3];
       UR1m[mn] = roR * aM;
       UR1m[mt1] = roR * vt1R;
@@ -348,7 +382,7 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
       double gUL1E = 0, gUR1E = 0, gUL1bt1 = 0, gUL1bt2 = 0, gUR1bt1 = 0, gUR1bt2 = 0;
       double gvt1L = 0, gvt2L = 0, gvt1R = 0, gvt2R = 0;
 
-      if (aL1 >= 0.0) {  // F(L*)
+      if (decide<MODE>(aL1 >= 0.0, code, tape::kLS)) {  // F(L*)
         for (int k = 0; k < 3; ++k) {
           gSL += gF[k] * (UL1m[k] - sL.Um[k]);
           gUL1m[k] += SL * gF[k];
@@ -365,7 +399,7 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
         gUL1bt2 += SL * gF[bt2];
         gL[bt2] -= SL * gF[bt2];
         for (int q = 0; q < 7; ++q) gsL.F[fl[q]] += gF[fl[q]];
-      } else if (aR1 <= 0.0) {  // F(R*)
+      } else if (decide<MODE>(aR1 <= 0.0, code, tape::kRS)) {  // F(R*)
         for (int k = 0; k < 3; ++k) {
           gSR += gF[k] * (UR1m[k] - sR.Um[k]);
           gUR1m[k] += SR * gF[k];
@@ -384,14 +418,14 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
         for (int q = 0; q < 7; ++q) gsR.F[fl[q]] += gF[fl[q]];
       } else {  // central states
         const double rLs = sqL, rRs = sqR;
-        const double ic = 1.0 / (rLs + rRs);
-        const double sg = std::copysign(1.0, Ubn);
+        const double ic = arcp(rLs + rRs);
+        const double sg = (MODE == tape::kNone) ? std::copysign(1.0, Ubn) : (bneg ? -1.0 : 1.0);
         const double at1 = ic * (rLs * vt1L + rRs * vt1R + (UR1bt1 - UL1bt1) * sg);
         const double at2 = ic * (rLs * vt2L + rRs * vt2R + (UR1bt2 - UL1bt2) * sg);
         const double U2bt1 = ic * (rLs * UR1bt1 + rRs * UL1bt1 + rLs * rRs * (vt1R - vt1L) * sg);
         const double U2bt2 = ic * (rLs * UR1bt2 + rRs * UL1bt2 + rLs * rRs * (vt2R - vt2L) * sg);
         double gat1 = 0, gat2 = 0, gU2bt1 = 0, gU2bt2 = 0, grLs = 0, grRs = 0, gic = 0;
-        const bool left = aM >= 0.0;
+        const bool left = decide<MODE>(aM >= 0.0, code, tape::kSSLeft);
         const double* S = left ? L : R;
         const Side& sS = left ? sL : sR;
         SideG& gsS = left ? gsL : gsR;
@@ -538,8 +572,8 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
         gaM += gUL1m[mn] * roL;
         gvt1L += gUL1m[mt1] * roL;
         gvt2L += gUL1m[mt2] * roL;
-        const double gnum = gUL1E / eL;
-        geL -= gUL1E * UL1E / eL;
+        const double gnum = gUL1E * ieL;
+        geL -= gUL1E * UL1E * ieL;
         gtL += gnum * sL.UE;
         gsL.UE += gnum * tL;
         gsL.pt -= gnum * L[vn];
@@ -594,8 +628,8 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
         gaM += gUR1m[mn] * roR;
         gvt1R += gUR1m[mt1] * roR;
         gvt2R += gUR1m[mt2] * roR;
-        const double gnum = gUR1E / eR;
-        geR -= gUR1E * UR1E / eR;
+        const double gnum = gUR1E * ieR;
+        geR -= gUR1E * UR1E * ieR;
         gtR += gnum * sR.UE;
         gsR.UE += gnum * tR;
         gsR.pt -= gnum * R[vn];
@@ -647,19 +681,23 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
       }
     }
     // ---- common tail: Alfven speeds, rho*, total pressure, aM, HLL state ----
-    double gaUbn = gaVL / sqL + gaVR / sqR;
-    gsqL -= gaVL * aVL / sqL;
-    gsqR -= gaVR * aVR / sqR;
-    groL += (sqL > 0.0) ? gsqL * 0.5 / sqL : 0.0;
-    groR += (sqR > 0.0) ? gsqR * 0.5 / sqR : 0.0;
-    // d|Bn|/dBn: the sign, and 0 at Bn == 0 (where a central difference sees no slope)
-    gUh[bn] += (Ubn > 0.0) ? gaUbn : ((Ubn < 0.0) ? -gaUbn : 0.0);
-    gL[kRO] += groL * tL / eL;
-    gtL += groL * L[kRO] / eL;
-    geL -= groL * roL / eL;
-    gR[kRO] += groR * tR / eR;
-    gtR += groR * R[kRO] / eR;
-    geR -= groR * roR / eR;
+    double gaUbn = gaVL * isqL + gaVR * isqR;
+    gsqL -= gaVL * aVL * isqL;
+    gsqR -= gaVR * aVR * isqR;
+    groL += (sqL > 0.0) ? gsqL * 0.5 * isqL : 0.0;
+    groR += (sqR > 0.0) ? gsqR * 0.5 * isqR : 0.0;
+    // d|Bn|/dBn: the sign; at Bn == 0 it is 0 when recomputed (a central
+    // difference there sees no slope) and the recorded sign under a tape
+    if (MODE == tape::kNone)
+      gUh[bn] += (Ubn > 0.0) ? gaUbn : ((Ubn < 0.0) ? -gaUbn : 0.0);
+    else
+      gUh[bn] += bneg ? -gaUbn : gaUbn;
+    gL[kRO] += groL * tL * ieL;
+    gtL += groL * L[kRO] * ieL;
+    geL -= groL * roL * ieL;
+    gR[kRO] += groR * tR * ieR;
+    gtR += groR * R[kRO] * ieR;
+    geR -= groR * roR * ieR;
     gSL += geL;
     gaM -= geL;
     gSR += geR;
@@ -673,8 +711,8 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
     gL[vn] -= gtL;
     gSR += gtR;
     gR[vn] -= gtR;
-    gUh[mn] += gaM / Uh[kRO];
-    gUh[kRO] -= gaM * aM / Uh[kRO];
+    gUh[mn] += gaM * iUr;
+    gUh[kRO] -= gaM * aM * iUr;
     for (int k = 0; k < 3; ++k) {
       gih += gUh[k] * NU[k];
       const double gN = ih * gUh[k];
@@ -708,7 +746,7 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
     gR[vn] += gSR;
   else
     gL[vn] += gSR;
-  const double gamax = (cf > 0.0) ? gcf * 0.5 / cf : 0.0;
+  const double gamax = gcf * 0.5 * icf;
   if (aRsel)
     gsR.a += gamax;
   else
@@ -717,53 +755,68 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
   side_adj<DIR>(R, gamma, r1, r2, sR, gsR, gR);
 }
 
-// minmod (type 1) / MC (type 2) reconstruction of one cell and its adjoint:
-// right = w0 - grad (state at the lower face), left = w0 + grad (upper face).
+// Selection code (tape::kLim*) of the minmod (type 1) / MC (type 2)
+// reconstruction of one cell, with the forward's tie rule (fmin2: the first
+// operand wins ties; opposite signs -> zero slope).
+OMHD_HD unsigned char recon_code(int type, double wm, double w0, double wp) {
+  const double gA = w0 - wm, gB = wp - w0;
+  if (std::signbit(gA) != std::signbit(gB)) return tape::kLimZero;
+  const double aA = std::fabs(gA), aB = std::fabs(gB);
+  if (type == 2) {
+    const double gC = 0.25 * (wp - wm);
+    const double m1 = (aB < aA) ? aB : aA;
+    if (std::fabs(gC) < m1)
+      return (unsigned char)(tape::kLimC | ((std::signbit(gA) != std::signbit(gC)) ? tape::kLimCNeg : 0));
+  }
+  return (aB < aA) ? tape::kLimB : tape::kLimA;
+}
+
+// Adjoint of one cell's reconstruction with a given selection code:
+// left = w0 + grad (upper face), right = w0 - grad (lower face), grad the
+// selected slope times 0.5 (minmod) or 1 (MC; gC = (wp - wm)/4 with its sign).
+OMHD_HD void recon_vjp_code(int type, unsigned char code, double gleft, double gright, double& gwm, double& gw0,
+                            double& gwp) {
+  gw0 += gleft + gright;
+  const double c = (type == 2) ? 1.0 : 0.5;
+  const double gg = c * (gleft - gright);
+  switch (code & 3) {
+    case tape::kLimA:
+      gw0 += gg;
+      gwm -= gg;
+      break;
+    case tape::kLimB:
+      gwp += gg;
+      gw0 -= gg;
+      break;
+    case tape::kLimC: {
+      const double k = (code & tape::kLimCNeg) ? -0.25 * gg : 0.25 * gg;
+      gwp += k;
+      gwm -= k;
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+// minmod (type 1) / MC (type 2) reconstruction of one cell and its adjoint,
+// selection recomputed from the cell and its neighbours.
 OMHD_HD void recon_vjp(int type, double wm, double w0, double wp, double gleft, double gright, double& gwm,
                        double& gw0, double& gwp) {
-  const double gA = w0 - wm, gB = wp - w0;
-  gw0 += gleft + gright;
-  const double ggrad = gleft - gright;
-  const double aA = std::fabs(gA), aB = std::fabs(gB);
-  if (std::signbit(gA) != std::signbit(gB)) return;  // grad = 0
-  if (type == 1) {
-    // grad = +-0.5*min(|gA|,|gB|) = 0.5*gA if |gA| picked (ties: first operand), else 0.5*gB
-    if (aB < aA) {
-      gwp += 0.5 * ggrad;
-      gw0 -= 0.5 * ggrad;
-    } else {
-      gw0 += 0.5 * ggrad;
-      gwm -= 0.5 * ggrad;
-    }
-  } else {
-    const double gC = 0.25 * (wp - wm), aC = std::fabs(gC);
-    const double m1 = (aB < aA) ? aB : aA;  // fmin2(fmin2(|gA|,|gB|),|gC|)
-    if (aC < m1) {
-      // grad = sign * |gC| = gC (same sign as gA, gB unless gC has the other sign)
-      const double s = std::copysign(1.0, gA) * std::copysign(1.0, gC);
-      gwp += s * 0.25 * ggrad;
-      gwm -= s * 0.25 * ggrad;
-    } else if (aB < aA) {
-      gwp += ggrad;
-      gw0 -= ggrad;
-    } else {
-      gw0 += ggrad;
-      gwm -= ggrad;
-    }
-  }
+  recon_vjp_code(type, recon_code(type, wm, w0, wp), gleft, gright, gwm, gw0, gwp);
 }
 
 // u2v (u2v.f90:24-27) adjoint: gU += (dw/dU)^T gw for w = (v, p, rho, B, psi).
 OMHD_HD void u2v_vjp(const double* U, double gamma, const double* gw, double* gU) {
-  const double ro = U[kRO];
-  const double v0 = U[0] / ro, v1 = U[1] / ro, v2 = U[2] / ro;
+  const double ro = U[kRO], ir = arcp(ro);
+  const double v0 = U[0] * ir, v1 = U[1] * ir, v2 = U[2] * ir;
   const double f1 = gamma - 1;
   const double gp = gw[kPR];
   // v_k = m_k/rho
-  gU[0] += gw[0] / ro;
-  gU[1] += gw[1] / ro;
-  gU[2] += gw[2] / ro;
-  gU[kRO] -= (gw[0] * v0 + gw[1] * v1 + gw[2] * v2) / ro;
+  gU[0] += gw[0] * ir;
+  gU[1] += gw[1] * ir;
+  gU[2] += gw[2] * ir;
+  gU[kRO] -= (gw[0] * v0 + gw[1] * v1 + gw[2] * v2) * ir;
   // p = f1*(E - 0.5*(v.m + B.B)) with v.m = |m|^2/rho
   gU[kEN] += f1 * gp;
   gU[0] -= f1 * gp * v0;

@@ -28,12 +28,19 @@ struct StageArgs {
   StepState* st;
   DevError* err;
   double cfl, dmin;     // for the end-of-step dt planning
+  // decision tape of this stage (taped FP64 HLLD launches only; see omhd_tape.h):
+  // limiter codes [2 directions][NV][cells], HLLD codes [2 directions][cells]
+  // indexed by the face's lower cell
+  unsigned char* tlim;
+  unsigned short* tface;
 };
 
 // launchers: return 0 or a CUDA error code
 int launch_stage2d_fp64(const StageArgs& a, cudaStream_t s);
 int launch_stage2d_parity(const StageArgs& a, cudaStream_t s);
 int launch_stage2d_mixed(const StageArgs& a, cudaStream_t s);
+// fp64 HLLD stage with a decision tape: mode tape::kRecord or tape::kReplay
+int launch_stage2d_fp64_tape(const StageArgs& a, int mode, cudaStream_t s);
 // ensemble launchers: tile_kind 0: 32x8, 1: 32x4, 2: 16x16, 3: 64x4 cells per CTA
 int launch_batch2d_fp64(int flux, int tile_kind, const StageArgs* args_dev, const int* tile_start_dev, int ngrids,
                         int total_tiles, int ctas, cudaStream_t s);

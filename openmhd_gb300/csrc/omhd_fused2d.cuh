@@ -80,7 +80,20 @@ __device__ __forceinline__ double eta_at(int kind, double x, double y, double z)
 // One stage on one tile (tile coordinates bxi, byi) of the grid described by
 // `a`; returns this thread's CFL speed of the updated cell (stage 2) or 0.
 // All threads of the CTA must call it (it synchronises the CTA).
-template <class T, int FLUX, class G>
+// canonical interior cell of a (possibly ghost or out-of-grid) index along an
+// axis of extent n, for decision-tape lookups: periodic ghosts wrap, other
+// indices clamp (their states are unused)
+__device__ __forceinline__ int tape_cell(int g, int n, bool periodic) {
+  if (periodic) {
+    const int P = n - 2;
+    int r = (g - 1) % P;
+    if (r < 0) r += P;
+    return r + 1;
+  }
+  return g < 1 ? 1 : (g > n - 2 ? n - 2 : g);
+}
+
+template <class T, int FLUX, class G, int TAPE = tape::kNone>
 __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int byi, unsigned char* smem_raw,
                                                double dt, double chd, double glmf) {
   constexpr int TX = G::TX, TY = G::TY, NT = G::NT, RX = G::RX, RY = G::RY;
@@ -167,12 +180,32 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
       dl = SLy;
       dr = SRy;
     }
+    if constexpr (TAPE == tape::kNone) {
 #pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      T l, r;
-      reconstruct_t<T, OMHD_FAST>(lm, W[v * PL + o - st], W[v * PL + o], W[v * PL + o + st], l, r);
-      dl[v * (q < NXS ? NXS : NYS) + qq] = l;
-      dr[v * (q < NXS ? NXS : NYS) + qq] = r;
+      for (int v = 0; v < NV; ++v) {
+        T l, r;
+        reconstruct_t<T, OMHD_FAST>(lm, W[v * PL + o - st], W[v * PL + o], W[v * PL + o + st], l, r);
+        dl[v * (q < NXS ? NXS : NYS) + qq] = l;
+        dr[v * (q < NXS ? NXS : NYS) + qq] = r;
+      }
+    } else {
+      // this cell's global index; x cells cx = 0..TX+1 of row cy, y cells
+      // cy = 0..TY+1 of column cx (the tile owns cx/cy = 1..TX/TY)
+      const bool xd = q < NXS;
+      const int cx = xd ? q % XS : qq % TX, cy = xd ? q / XS : qq / TX;
+      const int gi = xd ? gi0 - 1 + cx : gi0 + cx, gj = xd ? gj0 + cy : gj0 - 1 + cy;
+      const bool own = (xd ? (cx >= 1 && cx <= TX) : (cy >= 1 && cy <= TY)) && gi <= ix - 2 && gj <= jx - 2;
+      const size_t tc = (size_t)tape_cell(gi, ix, perx) + (size_t)ix * tape_cell(gj, jx, pery);
+      unsigned char* tl = a.tlim + (size_t)(xd ? 0 : 1) * NV * N;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double l, r;
+        unsigned char k = (TAPE == tape::kReplay) ? tl[v * N + tc] : 0;
+        reconstruct_fp64<OMHD_FAST, TAPE>(lm, W[v * PL + o - st], W[v * PL + o], W[v * PL + o + st], l, r, &k);
+        if (TAPE == tape::kRecord && own) tl[v * N + tc] = k;
+        dl[v * (xd ? NXS : NYS) + qq] = l;
+        dr[v * (xd ? NXS : NYS) + qq] = r;
+      }
     }
   }
   __syncthreads();
@@ -220,7 +253,16 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
         L[v] = SLx[v * NXS + cy * XS + fx];
         R[v] = SRx[v * NXS + cy * XS + fx + 1];
       }
-      riemann_flux<T, 1, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
+      if constexpr (TAPE == tape::kNone) {
+        riemann_flux<T, 1, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
+      } else {  // face between cells gi0-1+fx and gi0+fx of row gj0+cy
+        const int gl = gi0 - 1 + fx, gj = gj0 + cy;
+        const size_t tc = (size_t)(gl < 0 ? 0 : (gl > ix - 2 ? ix - 2 : gl)) + (size_t)ix * (gj > jx - 2 ? jx - 2 : gj);
+        unsigned k = (TAPE == tape::kReplay) ? a.tface[tc] : 0u;
+        riemann_flux<T, 1, FLUX, OMHD_FAST, TAPE>(L, R, ch, gam, r1, r2, Fo, &k);
+        if (TAPE == tape::kRecord && (fx >= 1 || gi0 == 1) && gl <= ix - 2 && gj <= jx - 2)
+          a.tface[tc] = (unsigned short)k;
+      }
       if (resist) {  // 2D_reconnection/flux_resistive.f90:266-283
         const int g = gi0 - 1 + fx, gj = gj0 + cy;
         if (g >= 0 && g <= ix - 2 && gj <= jx - 2) {
@@ -247,7 +289,16 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
         L[v] = SLy[v * NYS + fy * TX + cx];
         R[v] = SRy[v * NYS + (fy + 1) * TX + cx];
       }
-      riemann_flux<T, 2, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
+      if constexpr (TAPE == tape::kNone) {
+        riemann_flux<T, 2, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
+      } else {  // face between rows gj0-1+fy and gj0+fy of column gi0+cx
+        const int gl = gj0 - 1 + fy, gi = gi0 + cx;
+        const size_t tc = (size_t)(gi > ix - 2 ? ix - 2 : gi) + (size_t)ix * (gl < 0 ? 0 : (gl > jx - 2 ? jx - 2 : gl));
+        unsigned k = (TAPE == tape::kReplay) ? a.tface[N + tc] : 0u;
+        riemann_flux<T, 2, FLUX, OMHD_FAST, TAPE>(L, R, ch, gam, r1, r2, Fo, &k);
+        if (TAPE == tape::kRecord && (fy >= 1 || gj0 == 1) && gl <= jx - 2 && gi <= ix - 2)
+          a.tface[N + tc] = (unsigned short)k;
+      }
       if (resist) {  // 2D_reconnection/flux_resistive.f90:289-306
         const int gi = gi0 + cx, g = gj0 - 1 + fy;
         if (g >= 0 && g <= jx - 2 && gi <= ix - 2) {
@@ -333,7 +384,7 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
 }
 
 // one CTA per tile of one grid
-template <class T, int FLUX>
+template <class T, int FLUX, int TAPE = tape::kNone>
 __global__ void __launch_bounds__(GeoDefault::NT) k_stage2d(const StageArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red32[32];
@@ -344,8 +395,8 @@ __global__ void __launch_bounds__(GeoDefault::NT) k_stage2d(const StageArgs a) {
   if (threadIdx.x == 0) skip = st->done || *(volatile int*)&a.err->code;
   __syncthreads();
   if (skip) return;
-  const double vcell = stage2d_tile<T, FLUX, GeoDefault>(a, blockIdx.x, blockIdx.y, smem_raw, st->dt, st->ch,
-                                                         st->glm_f);
+  const double vcell = stage2d_tile<T, FLUX, GeoDefault, TAPE>(a, blockIdx.x, blockIdx.y, smem_raw, st->dt, st->ch,
+                                                               st->glm_f);
   if (a.stage == 2) {
     const double bm = block_max_pos(vcell, red32);
     StepConsts sc{a.cfl, a.dmin, a.dx, a.eta_kind};
@@ -402,17 +453,18 @@ __global__ void __launch_bounds__(G::NT) k_batch2d(const StageArgs* __restrict__
   }
 }
 
-template <class T, int FLUX>
+template <class T, int FLUX, int TAPE = tape::kNone>
 int launch_one(const StageArgs& a, cudaStream_t s) {
   const size_t bytes = GeoDefault::smem_bytes<T>();
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_stage2d<T, FLUX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_stage2d<T, FLUX, TAPE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e != cudaSuccess) return (int)e;
     configured = true;
   }
   dim3 grid((a.ix - 2 + GeoDefault::TX - 1) / GeoDefault::TX, (a.jx - 2 + GeoDefault::TY - 1) / GeoDefault::TY);
-  k_stage2d<T, FLUX><<<grid, GeoDefault::NT, bytes, s>>>(a);
+  k_stage2d<T, FLUX, TAPE><<<grid, GeoDefault::NT, bytes, s>>>(a);
   return (int)cudaGetLastError();
 }
 

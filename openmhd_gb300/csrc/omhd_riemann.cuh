@@ -11,41 +11,10 @@
 // multiply-adds.
 #pragma once
 #include "omhd_common.cuh"
+#include "omhd_fastmath.h"
+#include "omhd_tape.h"
 
 namespace omhd {
-
-// ---------------------------------------------------------------------------
-// FP64 division and square root on a GPU whose FP64 pipe issues ~0.5 T
-// instructions/s: an IEEE divide costs ~8.5 FP64-pipe instructions and a
-// square root ~10.  The performance variants (FAST = true) replace them by
-// Newton-Raphson iterations (Newton's method for f(y) = 1/y - x and
-// f(y) = 1/y^2 - x, quadratic convergence) started from hardware
-// approximations: rcp.approx.ftz.f64 (the special-function unit, ~20 bits)
-// and rsqrt.approx.ftz.f32 on the float-rounded argument (~22 bits).  Two
-// iterations give ~1 ulp; one reciprocal or one rsqrt is shared by every use
-// of the same denominator.  The parity variant (FAST = false) keeps the
-// reference's IEEE operations.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ double rcp_nr(double x) {
-  double y;
-  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-  double e = fma(-x, y, 1.0);
-  y = fma(y, e, y);
-  e = fma(-x, y, 1.0);
-  return fma(y, e, y);
-}
-
-__device__ __forceinline__ double rsqrt_nr(double x) {
-  const float xf = (float)x;
-  if (!(xf > 1.0e-37f && xf < 1.0e37f)) return 1.0 / sqrt(x);  // outside the float seed's range
-  float y0;
-  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y0) : "f"(xf));
-  double y = (double)y0;
-  double e = fma(-x * y, y, 1.0);
-  y = fma(0.5 * y, e, y);
-  e = fma(-x * y, y, 1.0);
-  return fma(0.5 * y, e, y);
-}
 
 // a / b and 1 / b under the variant's policy
 template <class T, bool FAST>
@@ -118,23 +87,62 @@ __device__ __forceinline__ double min_nonneg(double a, double b) {
 // +-2c otherwise, and 2c*min(...) is an exact power-of-two scaling, so the face
 // states equal the reference's bit for bit: w0 +- (+-2c)*m is one fused
 // multiply-add with an exactly representable product.
-template <bool FAST>
+//
+// Under a decision tape (TAPE = tape::kRecord / kReplay, minmod and MC only)
+// the selection is recorded in *code, or taken from it: a replayed selection
+// is applied as the linear map it stands for (c*gA, c*gB or +-gC), which
+// equals the recorded arithmetic bit for bit while no slope changes sign.
+template <bool FAST, int TAPE = tape::kNone>
 __device__ __forceinline__ void reconstruct_fp64(int type, double wm, double w0, double wp, double& left,
-                                                 double& right) {
+                                                 double& right, unsigned char* code = nullptr) {
+  if constexpr (TAPE == tape::kReplay) {
+    const double c = (type == LM_MC) ? 1.0 : 0.5;
+    const unsigned char k = *code;
+    double sel = 0.0, cc = c;
+    switch (k & 3) {
+      case tape::kLimA: sel = w0 - wm; break;
+      case tape::kLimB: sel = wp - w0; break;
+      case tape::kLimC:
+        sel = 0.25 * (wp - wm);
+        if (k & tape::kLimCNeg) cc = -c;
+        break;
+      default: cc = 0.0;
+    }
+    left = fma(cc, sel, w0);
+    right = fma(-cc, sel, w0);
+    return;
+  }
   if constexpr (FAST) {
     if (type == LM_MINMOD || type == LM_MC) {
       const double gA = (w0 - wm);
       const double gB = (wp - w0);
       const long long sa = __double_as_longlong(gA), sb = __double_as_longlong(gB);
+      const long long ia = __double_as_longlong(fabs(gA)), ib = __double_as_longlong(fabs(gB));
       double m = min_nonneg(fabs(gA), fabs(gB));
       double c = 0.5;  // minmod: (0.25 + 0.25)
+      bool pickC = false;
+      double gC = 0.0;
       if (type == LM_MC) {
-        m = min_nonneg(m, fabs(0.25 * (wp - wm)));
+        gC = 0.25 * (wp - wm);
+        const long long ic = __double_as_longlong(fabs(gC));
+        pickC = ic < __double_as_longlong(m);
+        m = min_nonneg(m, fabs(gC));
         c = 1.0;  // MC: (0.5 + 0.5)
       }
-      const double s = ((sa ^ sb) < 0) ? 0.0 : copysign(c, gA);
+      const bool zero = (sa ^ sb) < 0;
+      const double s = zero ? 0.0 : copysign(c, gA);
       left = fma(s, m, w0);
       right = fma(-s, m, w0);
+      if constexpr (TAPE == tape::kRecord) {
+        unsigned char k;
+        if (zero)
+          k = tape::kLimZero;
+        else if (pickC)
+          k = (unsigned char)(tape::kLimC | (((sa ^ __double_as_longlong(gC)) < 0) ? tape::kLimCNeg : 0));
+        else
+          k = (ib < ia) ? tape::kLimB : tape::kLimA;
+        *code = k;
+      }
       return;
     }
   }
@@ -153,9 +161,14 @@ __device__ __forceinline__ void reconstruct_t(int type, T wm, T w0, T wp, T& lef
 //   LLF :89-148, HLL :153-221, HLLC :226-347, HLLD :352-585 (HLLC-G fallback
 //   :447-476), LHLLD :590-789; GLM fluxes for Bn and psi :580-581.
 // r1 = 1/(gamma-1), r2 = gamma/(gamma-1) are passed in (flux_solver.f90:38-39).
-template <class T, int DIR, int TYPE, bool FAST = false>
+//
+// Under a decision tape (TAPE != tape::kNone; HLLD only) every comparison that
+// selects a wave speed, a region or a sign is recorded in *code or replayed
+// from it (tape::kArSel ... tape::kClampR); the arithmetic is unchanged.
+template <class T, int DIR, int TYPE, bool FAST = false, int TAPE = tape::kNone>
 __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV], T ch, T gamma, T r1,
-                                             T r2, T (&Fo)[NV]) {
+                                             T r2, T (&Fo)[NV], unsigned* code = nullptr) {
+  using tape::decide;
   constexpr int vn = VX + (DIR - 1) % 3, vt1 = VX + DIR % 3, vt2 = VX + (DIR + 1) % 3;
   constexpr int bn = BX + (DIR - 1) % 3, bt1 = BX + DIR % 3, bt2 = BX + (DIR + 1) % 3;
   constexpr int mn = MX + (DIR - 1) % 3, mt1 = MX + DIR % 3, mt2 = MX + (DIR + 1) % 3;
@@ -191,7 +204,13 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   if (TYPE == FX_LLF) {
     aL = sqrt(div_<T, FAST>((f1 + B2) + sqrt((f1 + B2) * (f1 + B2) - f1 * f2), 2 * L[RO]));
   } else {
-    aL = div_<T, FAST>((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f1 * f2, T(0))), 2 * L[RO]);
+    if constexpr (TAPE != tape::kNone) {
+      const T D = (f1 + B2) * (f1 + B2) - f1 * f2;
+      const bool cl = decide<TAPE>(T(0) > D, code, tape::kClampL);
+      aL = div_<T, FAST>((f1 + B2) + sqrt(cl ? T(0) : D), 2 * L[RO]);
+    } else {
+      aL = div_<T, FAST>((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f1 * f2, T(0))), 2 * L[RO]);
+    }
     ptL = L[PR] + T(0.5) * B2;
     if (TYPE == FX_LHLLD) {
       const T g1 = L[RO] * v2;
@@ -219,7 +238,13 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   if (TYPE == FX_LLF) {
     aR = sqrt(div_<T, FAST>((f1 + B2) + sqrt((f1 + B2) * (f1 + B2) - f1 * f2), 2 * R[RO]));
   } else {
-    aR = div_<T, FAST>((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f1 * f2, T(0))), 2 * R[RO]);
+    if constexpr (TAPE != tape::kNone) {
+      const T D = (f1 + B2) * (f1 + B2) - f1 * f2;
+      const bool cl = decide<TAPE>(T(0) > D, code, tape::kClampR);
+      aR = div_<T, FAST>((f1 + B2) + sqrt(cl ? T(0) : D), 2 * R[RO]);
+    } else {
+      aR = div_<T, FAST>((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f1 * f2, T(0))), 2 * R[RO]);
+    }
     ptR = R[PR] + T(0.5) * B2;
     if (TYPE == FX_LHLLD) {
       const T g1 = R[RO] * v2;
@@ -282,13 +307,13 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
       f1 = fmin2(T(1), div_<T, FAST>(fmax2(aL1, aR1), fmax2(aL, aR)));
       psi = 2 * sqrt(f1) - f1;
     }
-    f1 = sqrt(fmax2(aL, aR));
-    aL = fmin2(L[vn], R[vn]) - f1;
-    aR = fmax2(L[vn], R[vn]) + f1;
-    if (aL >= T(0)) {
+    f1 = sqrt(decide<TAPE>(aR > aL, code, tape::kArSel) ? aR : aL);  // fmax2(aL, aR)
+    aL = (decide<TAPE>(R[vn] < L[vn], code, tape::kMinR) ? R[vn] : L[vn]) - f1;  // fmin2
+    aR = (decide<TAPE>(R[vn] > L[vn], code, tape::kMaxR) ? R[vn] : L[vn]) + f1;  // fmax2
+    if (decide<TAPE>(aL >= T(0), code, tape::kFL)) {
 #pragma unroll
       for (int v = 0; v < NV; ++v) Fo[v] = FL[v];
-    } else if (aR <= T(0)) {
+    } else if (decide<TAPE>(aR <= T(0), code, tape::kFR)) {
 #pragma unroll
       for (int v = 0; v < NV; ++v) Fo[v] = FR[v];
     } else {
@@ -315,9 +340,13 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
         rsL = rsqrt_nr(roL);
         rsR = rsqrt_nr(roR);
       }
-      const T aVL = (FAST && sizeof(T) == 8) ? fabs(Uh[bn]) * rsL : fabs(Uh[bn]) / sqrt(roL);
-      const T aVR = (FAST && sizeof(T) == 8) ? fabs(Uh[bn]) * rsR : fabs(Uh[bn]) / sqrt(roR);
-      if (TYPE == FX_HLLD && ((aL >= (aM - hllg_factor * aVL)) || ((aM + hllg_factor * aVR) >= aR))) {
+      // |Bn| and sign(1, Bn) from one recorded sign bit under a tape
+      const bool bneg = decide<TAPE>(signbit(Uh[bn]) != 0, code, tape::kBnNeg);
+      const T aBn = (TAPE == tape::kNone) ? fabs(Uh[bn]) : (bneg ? -Uh[bn] : Uh[bn]);
+      const T aVL = (FAST && sizeof(T) == 8) ? aBn * rsL : aBn / sqrt(roL);
+      const T aVR = (FAST && sizeof(T) == 8) ? aBn * rsR : aBn / sqrt(roR);
+      if (TYPE == FX_HLLD && decide<TAPE>((aL >= (aM - hllg_factor * aVL)) || ((aM + hllg_factor * aVR) >= aR),
+                                          code, tape::kG)) {
         // HLLC-G fallback :450-476
         f2 = aL * aR;
         Fo[bt1] = f1 * (aR * FL[bt1] - aL * FR[bt1] + f2 * (R[bt1] - L[bt1]));
@@ -328,7 +357,10 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
                        Uh[bn] * (vBL - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])), (aL - aM));
         const T enR = div_<T, FAST>(((aR - R[vn]) * UR[EN] - ptR * R[vn] + pt * aM +
                        Uh[bn] * (vBR - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])), (aR - aM));
-        f1 = T(0.5) + fsign(T(0.5), aM);
+        if constexpr (TAPE != tape::kNone)
+          f1 = decide<TAPE>(signbit(aM) == 0, code, tape::kGLeft) ? T(1) : T(0);  // 0.5 + sign(0.5, aM)
+        else
+          f1 = T(0.5) + fsign(T(0.5), aM);
         f2 = T(1) - f1;
         Fo[mn] = f1 * (aL * (roL * aM - UL[mn]) + FL[mn]) + f2 * (aR * (roR * aM - UR[mn]) + FR[mn]);
         Fo[mt1] = f1 * (aL * (roL * at1 - UL[mt1]) + FL[mt1]) + f2 * (aR * (roR * at1 - UR[mt1]) + FR[mt1]);
@@ -365,13 +397,13 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
         UR1[mt2] = roR * vt2R;
         aL1 = aM - aVL;
         aR1 = aM + aVR;
-        if (aL1 >= T(0)) {  // F(L*) :514-519
+        if (decide<TAPE>(aL1 >= T(0), code, tape::kLS)) {  // F(L*) :514-519
 #pragma unroll
           for (int v = MX; v <= EN; ++v) Fo[v] = aL * (UL1[v] - UL[v]) + FL[v];
           Fo[RO] = aL * (UL1[RO] - L[RO]) + FL[RO];
           Fo[bt1] = aL * (UL1[bt1] - L[bt1]) + FL[bt1];
           Fo[bt2] = aL * (UL1[bt2] - L[bt2]) + FL[bt2];
-        } else if (aR1 <= T(0)) {  // F(R*) :522-527
+        } else if (decide<TAPE>(aR1 <= T(0), code, tape::kRS)) {  // F(R*) :522-527
 #pragma unroll
           for (int v = MX; v <= EN; ++v) Fo[v] = aR * (UR1[v] - UR[v]) + FR[v];
           Fo[RO] = aR * (UR1[RO] - R[RO]) + FR[RO];
@@ -382,12 +414,12 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
           const T roLs = (FAST && sizeof(T) == 8) ? roL * rsL : sqrt(roL);
           const T roRs = (FAST && sizeof(T) == 8) ? roR * rsR : sqrt(roR);
           f1 = rcp_<T, FAST>(roLs + roRs);
-          f2 = fsign(T(1), Uh[bn]);
+          f2 = (TAPE == tape::kNone) ? fsign(T(1), Uh[bn]) : (bneg ? T(-1) : T(1));
           const T at1 = f1 * (roLs * vt1L + roRs * vt1R + (UR1[bt1] - UL1[bt1]) * f2);
           const T at2 = f1 * (roLs * vt2L + roRs * vt2R + (UR1[bt2] - UL1[bt2]) * f2);
           U2[bt1] = f1 * (roLs * UR1[bt1] + roRs * UL1[bt1] + roLs * roRs * (vt1R - vt1L) * f2);
           U2[bt2] = f1 * (roLs * UR1[bt2] + roRs * UL1[bt2] + roLs * roRs * (vt2R - vt2L) * f2);
-          if (aM >= T(0)) {  // F(L**)
+          if (decide<TAPE>(aM >= T(0), code, tape::kSSLeft)) {  // F(L**)
             U2[RO] = roL;
             U2[EN] = UL1[EN] - roLs * (vt1L * UL1[bt1] + vt2L * UL1[bt2] - at1 * U2[bt1] - at2 * U2[bt2]) * f2;
             U2[mn] = roL * aM;

@@ -6,7 +6,8 @@
   walls, minmod and MC;
 - checkpoint spacing does not change the gradient (bit for bit);
 - KH dJ/dvy0 with J = sum By^2 agrees with central finite differences of
-  the forward along seeded directions.
+  the forward along seeded directions (plain, at a step small enough to
+  cross no kink, and frozen-decision replay at eps = 1e-6).
 """
 import math
 
@@ -133,13 +134,67 @@ def test_kh_gradient_against_finite_differences(cuda_lib):
     assert worst < 1e-6, worst
 
 
+def test_record_and_replay(cuda_lib):
+    """Recording the decision tape changes nothing (bit for bit); replaying it
+    from the same U0 reproduces the run to rounding (the replaying kernel is a
+    separate instantiation, free to contract multiply-adds differently)."""
+    from openmhd_gb300.adjoint import AdjointRun
+
+    cfg = small_cfg("kh_walls_minmod", 70, 38)
+    U0 = torch.from_numpy(smooth_state(38, 70, 5)).cuda()
+    run = AdjointRun(cfg, 6, 4)
+    a = run.forward(U0).cpu()
+    b = run.record(U0).cpu()
+    c = run.replay(U0).cpu()
+    run.sync()
+    assert torch.equal(a, b)
+    scale = b.abs().amax(dim=(1, 2), keepdim=True).clamp_min(1e-300)
+    assert float(((c - b).abs() / scale).max()) < 1e-12
+    d = run.replay(U0 * (1 + 1e-7)).cpu()
+    assert not torch.equal(c, d)
+
+
+def test_kh_gradient_against_frozen_finite_differences(cuda_lib):
+    """KH dJ/dvy0 (J = sum By^2) against central differences, eps = 1e-6, of
+    the forward with the recorded decisions frozen (replay): exact up to
+    O(eps^2) and rounding, however many limiter kinks +-eps would cross."""
+    from openmhd_gb300 import Solver, kelvin_helmholtz
+    from openmhd_gb300.adjoint import AdjointRun, kh_state
+
+    cfg, model = kelvin_helmholtz(64, 32, precision="fp64")
+    base = torch.from_numpy(Solver(cfg).init_model(model).get_state_numpy()).cuda()
+    vy0 = (base[1, 1:-1, 1:-1] / base[4, 1:-1, 1:-1]).clone()
+    run = AdjointRun(cfg, 40, 8)
+    vy = vy0.clone().requires_grad_(True)
+    J = kh_objective(run, base, vy)
+    J.backward()
+    grad = vy.grad.detach()
+    with torch.no_grad():
+        run.record(kh_state(base, vy0))
+
+        def Jf(v):
+            return float((run.replay(kh_state(base, v))[6, 1:-1, 1:-1] ** 2).sum())
+
+        rng = np.random.default_rng(11)
+        eps = 1e-6
+        worst = 0.0
+        for _ in range(4):
+            d = torch.from_numpy(rng.standard_normal(tuple(vy0.shape))).cuda()
+            fd = (Jf(vy0 + eps * d) - Jf(vy0 - eps * d)) / (2 * eps)
+            ad = float((grad * d).sum())
+            worst = max(worst, abs(fd - ad) / max(abs(fd), 1e-300))
+    assert worst < 1e-6, worst
+
+
 def test_memory_report(cuda_lib):
     from openmhd_gb300.adjoint import AdjointRun
 
     cfg = small_cfg("periodic_mc", 34, 30)
     run = AdjointRun(cfg, 100, 10)
-    S = 9 * cfg.ix * cfg.jx * 8
+    n = cfg.ix * cfg.jx
+    S = 9 * n * 8
+    tape = 10 * 2 * (2 * 9 * n + 2 * 2 * n)  # segment tape: 10 steps x 2 stages
     # 10 checkpoints + 2 x 10 segment states + 10 state-sized work arrays + step log
-    assert run.memory_bytes >= S * (10 + 20 + 10) + 3 * 100 * 8
-    assert run.memory_bytes < S * (10 + 20 + 10) + 3 * 100 * 8 + 4096
+    assert run.memory_bytes >= S * (10 + 20 + 10) + 3 * 100 * 8 + tape
+    assert run.memory_bytes < S * (10 + 20 + 10) + 3 * 100 * 8 + tape + 4096
     assert math.isfinite(run.memory_bytes)
