@@ -233,6 +233,7 @@ def run_ours(args):
         t_fp64 = float(tt.item())
     value = ws * cells * args.steps / t_fp64
     U64 = s.get_state_numpy()
+    div_b = _div_b_max(s.U, cfg.dx, cfg.dy)
 
     # ---- FP32-mixed on the same workload (same warm-up + steps) ----
     cfgm, _ = kelvin_helmholtz(NX, NY, precision="mixed")
@@ -300,6 +301,7 @@ def run_ours(args):
                    "l2": "state 605 MB > 129 MB L2: no flush needed", "parallelism": f"replicas{ws}"},
         "roofline": roofline,
         "gpu_launches": 2 * args.steps,
+        "max_div_b": div_b,
         "e2e": e2e,
         "clocks": clk.summary(),
         "mixed": {"value": ws * cells * args.steps / t_mx, "speedup_vs_fp64": t_fp64 / t_mx,
@@ -311,6 +313,8 @@ def run_ours(args):
         line["batched"] = run_batched(args)
     if not args.no_adjoint:
         line["adjoint"] = run_adjoint(args)
+    if not args.no_3d:
+        line["harris3d"] = run_3d(args)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"], _ = cpu_baseline(steps_budget_s=10.0)
     if rank == 0:
@@ -325,8 +329,10 @@ def run_ours(args):
 def run_batched(args):
     """128-member ensemble (seeded sizes in {128..1024}^2, half OT, half KH),
     FP32-mixed, one persistent batched kernel per RK stage, autotuned tiling,
-    K steps replayed as one CUDA graph; per-member error against the same
-    ensemble in FP64 after the same number of steps."""
+    K steps replayed as one CUDA graph.  Every member runs 500 steps in all;
+    the per-member error is against the same ensemble run in FP64 for the
+    same 500 steps, whose K-step time (same tiling, stream launches) is the
+    FP64 batched throughput."""
     import numpy as np
     import torch
 
@@ -347,10 +353,23 @@ def run_batched(args):
     e1.synchronize()
     infos = ens.sync()
     t = e0.elapsed_time(e1) / 1e3
-    total_steps = tuned_steps + 2 * args.steps
+    # every member runs BATCH_STEPS steps in all; the error is taken there
+    rest = BATCH_STEPS - tuned_steps - 2 * args.steps
+    if rest > 0:
+        ens.step(rest)
+        infos = ens.sync()
+    total_steps = max(BATCH_STEPS, tuned_steps + 2 * args.steps)
     cfg64, _ = batched_problem_set(128, seed=0, precision="fp64")
     ref = Ensemble(cfg64).init_models(models)
-    ref.step(total_steps)
+    ref.set_tiling(kind, cps)
+    ref.step(3)
+    ref.sync()
+    e0.record(ref.stream)
+    ref.step(args.steps)
+    e1.record(ref.stream)
+    e1.synchronize()
+    t64 = e0.elapsed_time(e1) / 1e3
+    ref.step(total_steps - 3 - args.steps)
     ref.sync()
     errs = []
     for i in range(len(cfgs)):
@@ -359,6 +378,7 @@ def run_batched(args):
         errs.append(float(np.max(scaled_l1(a, b))))
     del ref
     return {"value": ens.cells * args.steps / t, "unit": "cell-updates/s", "members": len(cfgs),
+            "fp64_batched_value": ens.cells * args.steps / t64, "speedup_vs_fp64_batched": t64 / t,
             "cells": ens.cells, "precision": "mixed", "tile_kind": kind, "ctas_per_sm": cps,
             "tile": ["32x8", "32x4", "16x16", "64x4"][kind], "ms_per_step": 1e3 * t / args.steps,
             "steps_compared": total_steps, "max_member_scaled_l1_vs_fp64": max(errs),
@@ -366,7 +386,84 @@ def run_batched(args):
             "dt_range": [min(x.dt for x in infos), max(x.dt for x in infos)]}
 
 
+H3_NX, H3_NY, H3_NZ = 512, 256, 512
+
+
+def _scaled_l1_t(a, b):
+    """scaled_l1 (openmhd_gb300.metrics) on device tensors (9, ...)."""
+    import torch
+
+    a = a.reshape(9, -1)
+    b = b.reshape(9, -1)
+    num = (a - b).abs().sum(dim=1)
+    m = torch.sqrt((2.0 * b[4] * b[3]).abs()).sum()
+    B = torch.sqrt((b[5:8] ** 2).sum(dim=0)).sum()
+    den = torch.stack([m, m, m, b[3].abs().sum(), b[4].abs().sum(), B, B, B, B])
+    floor = torch.clamp(den.max(), min=1e-300) * 1e-12
+    return (num / torch.maximum(den, floor)).cpu().tolist()
+
+
+def _div_b_max(U, dx, dy, dz=None):
+    """max |div B| over the interior, centred differences (the reference's
+    diagnostic form; GLM keeps it bounded rather than zero)."""
+    if U.dim() == 3:
+        d = (U[5, 1:-1, 2:] - U[5, 1:-1, :-2]) / (2 * dx) + (U[6, 2:, 1:-1] - U[6, :-2, 1:-1]) / (2 * dy)
+    else:
+        d = ((U[5, 1:-1, 1:-1, 2:] - U[5, 1:-1, 1:-1, :-2]) / (2 * dx)
+             + (U[6, 1:-1, 2:, 1:-1] - U[6, 1:-1, :-2, 1:-1]) / (2 * dy)
+             + (U[7, 2:, 1:-1, 1:-1] - U[7, :-2, 1:-1, 1:-1]) / (2 * dz))
+    return float(d.abs().max())
+
+
+def run_3d(args):
+    """3D resistive Harris sheet 512 x 256 x 512 (x, y periodic, z conducting
+    walls, HLLD + MC + GLM + resistive fluxes), FP64 and FP32-mixed on the
+    same steps: cell-updates/s, HBM GB/s against the 360 B per cell-update of
+    the fused two-stage design, and the mixed path's error against FP64."""
+    import torch
+
+    from openmhd_gb300 import Solver, harris3d
+
+    steps = max(3, min(args.steps, 20))
+    warm = 2
+    out = {"workload": f"harris3d_{H3_NX}x{H3_NY}x{H3_NZ}_hlld_mc_glm_resistive_tvdrk2", "steps": steps,
+           "warmup": warm}
+    states = {}
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    peaks, peak_src = _peaks()
+    for prec in ("fp64", "mixed"):
+        cfg, model = harris3d(H3_NX, H3_NY, H3_NZ, precision=prec)
+        s = Solver(cfg).init_model(model)
+        s.step(warm)
+        s.sync()
+        torch.cuda.synchronize()
+        e0.record(s.stream)
+        s.step(steps)
+        e1.record(s.stream)
+        e1.synchronize()
+        info = s.sync()
+        t = e0.elapsed_time(e1) / 1e3
+        cells = cfg.interior_cells
+        gbs = BYTES_PER_CELL_UPDATE_2D * cells * steps / t / 1e9
+        out[prec] = {"value": cells * steps / t, "unit": "cell-updates/s", "ms_per_step": 1e3 * t / steps,
+                     "hbm_gbs_algorithmic": gbs, "hbm_frac": gbs / peaks.get("hbm_gbs", 1.0),
+                     "hbm_peak_source": peak_src, "status": info.status, "launches_per_step": 2}
+        if prec == "fp64":
+            out[prec]["max_div_b"] = _div_b_max(s.U, cfg.dx, cfg.dy, cfg.dz)
+        states[prec] = s
+    out["mixed"]["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    from openmhd_gb300.metrics import VAR_NAMES
+
+    out["mixed"]["scaled_l1_vs_fp64"] = dict(zip(VAR_NAMES, _scaled_l1_t(states["mixed"].U, states["fp64"].U)))
+    out["mixed"]["steps_compared"] = warm + steps
+    del states
+    torch.cuda.empty_cache()
+    return out
+
+
 ADJ_NX, ADJ_NY, ADJ_STEPS, ADJ_EVERY = 512, 256, 400, 20
+BATCH_STEPS = 500  # steps every ensemble member runs (the error is taken there)
 
 
 def run_adjoint(args, ndir: int = 16, eps: float = 1e-6):
@@ -543,6 +640,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-3d", action="store_true")
     ap.add_argument("--adjoint-only", action="store_true", help="run the adjoint leg alone")
     ap.add_argument("--profile", action="store_true", help="small fixed run for profiler captures")
     ap.add_argument("--nx", type=int, default=NX)

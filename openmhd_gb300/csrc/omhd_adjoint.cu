@@ -343,7 +343,8 @@ struct omhd_adjoint {
   unsigned short* fullTf = nullptr;
   double* Uw = nullptr;      // working state of the forward runs
   double* U1w = nullptr;     // stage buffer of the plain forward run
-  double* logd = nullptr;    // 3 * nsteps
+  double* logd = nullptr;    // 3 * nsteps: {dt, ch, glm factor} of the last forward run
+  double* tlog = nullptr;    // 3 * nsteps: the same, of the recorded run (replay takes these)
   double* W = nullptr;       // primitives of the current stage input
   double* gUp = nullptr;     // 2 * NV planes
   double* gLo = nullptr;     // 2 * NV planes
@@ -449,7 +450,7 @@ int run_forward(omhd_adjoint* a, const double* U0, double* UN, int mode) {
     }
     if (r) break;
     if (mode == tape::kReplay)
-      k_force_step<<<1, 1, 0, a->stream>>>(s->st, a->logd + 3 * (size_t)k);
+      k_force_step<<<1, 1, 0, a->stream>>>(s->st, a->tlog + 3 * (size_t)k);
     else
       k_log_step<<<1, 1, 0, a->stream>>>(s->st, a->logd + 3 * (size_t)k);
     r = acerr(a, cudaGetLastError(), "step record kernel");
@@ -529,8 +530,8 @@ int omhd_adjoint_create(const omhd_config* cfg, int nsteps, int checkpoint_every
 int omhd_adjoint_destroy(omhd_adjoint* a) {
   if (!a) return OMHD_OK;
   if (a->s) omhd_solver_destroy(a->s);
-  void* bufs[] = {a->ck,   a->segU, a->segU1, a->segTl,  a->segTf,  a->fullTl, a->fullTf, a->Uw, a->U1w,
-                  a->logd, a->W,    a->gUp,   a->gLo,    a->lam[0], a->lam[1], a->lam[2], a->ckst};
+  void* bufs[] = {a->ck,   a->segU, a->segU1, a->segTl,  a->segTf,  a->fullTl, a->fullTf, a->Uw,  a->U1w,
+                  a->logd, a->tlog, a->W,    a->gUp,    a->gLo,    a->lam[0], a->lam[1], a->lam[2], a->ckst};
   for (void* p : bufs)
     if (p) cudaFree(p);
   delete a;
@@ -557,6 +558,7 @@ int omhd_adjoint_record(omhd_adjoint* a, const double* U0, double* UN) {
   if (!a->fullTl) {
     r = amalloc(a, &a->fullTl, 2 * tl_stride(a) * a->nsteps, "tape allocation");
     r = r ? r : amalloc(a, &a->fullTf, 2 * tf_stride(a) * a->nsteps, "tape allocation");
+    r = r ? r : amalloc(a, &a->tlog, 3 * (size_t)a->nsteps, "tape log allocation");
     r = r ? r : acerr(a, cudaMemsetAsync(a->fullTl, 0, 2 * tl_stride(a) * a->nsteps, a->stream), "tape clear");
     r = r ? r
           : acerr(a, cudaMemsetAsync(a->fullTf, 0, sizeof(unsigned short) * 2 * tf_stride(a) * a->nsteps, a->stream),
@@ -565,6 +567,10 @@ int omhd_adjoint_record(omhd_adjoint* a, const double* U0, double* UN) {
   }
   a->have_forward = a->have_tape = false;
   r = run_forward(a, U0, UN, tape::kRecord);
+  r = r ? r
+        : acerr(a, cudaMemcpyAsync(a->tlog, a->logd, sizeof(double) * 3 * a->nsteps, cudaMemcpyDeviceToDevice,
+                                   a->stream),
+                "tape log copy");
   if (!r) a->have_forward = a->have_tape = true;
   return r;
 }

@@ -203,6 +203,7 @@ class Solver:
         torch.cuda.current_stream().synchronize()
         mc = m.to_c()
         self._check(self.lib.omhd_solver_init_model(self._h, C.byref(mc)))
+        torch.cuda.current_stream().wait_stream(self.stream)  # U is read on the caller's stream next
         return self
 
     def put_state(self, U, t: float = 0.0):
@@ -243,7 +244,11 @@ class Solver:
 
     # -- stepping --
     def step(self, n: int = 1):
+        import torch
+
+        self.stream.wait_stream(torch.cuda.current_stream())  # the caller may have written U
         self._check(self.lib.omhd_solver_step(self._h, int(n)))
+        torch.cuda.current_stream().wait_stream(self.stream)
         return self
 
     def step_graph(self, n: int, replays: int = 1):
