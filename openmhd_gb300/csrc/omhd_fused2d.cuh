@@ -376,7 +376,8 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
         const double f1 = gamma * pr;
         const double vfx = fast_speed<double, OMHD_FAST>(f1, B2, out[BX], ro);
         const double vfy = fast_speed<double, OMHD_FAST>(f1, B2, out[BY], ro);
-        vcell = fmax2(fabs(vx) + vfx, fabs(vy) + vfy);
+        const double sx = fabs(vx) + vfx, sy = fabs(vy) + vfy;
+        vcell = lt_<double, OMHD_FAST>(sx, sy) ? sy : sx;  // fmax2(sx, sy)
       }
     }
   }

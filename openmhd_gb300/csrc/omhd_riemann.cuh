@@ -16,6 +16,42 @@
 
 namespace omhd {
 
+// Comparisons of the FP64 performance variants on the integer pipe (the FP64
+// pipe is the bottleneck; a floating-point compare or min/max occupies it like
+// an FMA).  Each returns the IEEE comparison's truth value (signed zeros
+// compare equal; NaN does not occur on the path), so results are bit-identical.
+__device__ __forceinline__ long long okey(double x) {  // order-preserving integer key
+  long long b = __double_as_longlong(x);
+  b = (b == (long long)0x8000000000000000ULL) ? 0 : b;  // -0 == +0
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+template <class T, bool FAST>
+__device__ __forceinline__ bool ge0_(T x) {  // x >= 0
+  if constexpr (FAST && sizeof(T) == 8) {
+    const long long b = __double_as_longlong(double(x));
+    return b >= 0 || b == (long long)0x8000000000000000ULL;
+  }
+  return x >= T(0);
+}
+template <class T, bool FAST>
+__device__ __forceinline__ bool le0_(T x) {  // x <= 0
+  if constexpr (FAST && sizeof(T) == 8) return __double_as_longlong(double(x)) <= 0;
+  return x <= T(0);
+}
+template <class T, bool FAST>
+__device__ __forceinline__ bool lt0_(T x) {  // x < 0
+  if constexpr (FAST && sizeof(T) == 8) {
+    const long long b = __double_as_longlong(double(x));
+    return b < 0 && b != (long long)0x8000000000000000ULL;
+  }
+  return x < T(0);
+}
+template <class T, bool FAST>
+__device__ __forceinline__ bool lt_(T a, T b) {  // a < b
+  if constexpr (FAST && sizeof(T) == 8) return okey(double(a)) < okey(double(b));
+  return a < b;
+}
+
 // a / b and 1 / b under the variant's policy
 template <class T, bool FAST>
 __device__ __forceinline__ T rcp_(T b) {
@@ -204,12 +240,10 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   if (TYPE == FX_LLF) {
     aL = sqrt(div_<T, FAST>((f1 + B2) + sqrt((f1 + B2) * (f1 + B2) - f1 * f2), 2 * L[RO]));
   } else {
-    if constexpr (TAPE != tape::kNone) {
+    {  // fmax2(D, 0)
       const T D = (f1 + B2) * (f1 + B2) - f1 * f2;
-      const bool cl = decide<TAPE>(T(0) > D, code, tape::kClampL);
+      const bool cl = decide<TAPE>(lt0_<T, FAST>(D), code, tape::kClampL);
       aL = div_<T, FAST>((f1 + B2) + sqrt(cl ? T(0) : D), 2 * L[RO]);
-    } else {
-      aL = div_<T, FAST>((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f1 * f2, T(0))), 2 * L[RO]);
     }
     ptL = L[PR] + T(0.5) * B2;
     if (TYPE == FX_LHLLD) {
@@ -238,12 +272,10 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   if (TYPE == FX_LLF) {
     aR = sqrt(div_<T, FAST>((f1 + B2) + sqrt((f1 + B2) * (f1 + B2) - f1 * f2), 2 * R[RO]));
   } else {
-    if constexpr (TAPE != tape::kNone) {
+    {  // fmax2(D, 0)
       const T D = (f1 + B2) * (f1 + B2) - f1 * f2;
-      const bool cl = decide<TAPE>(T(0) > D, code, tape::kClampR);
+      const bool cl = decide<TAPE>(lt0_<T, FAST>(D), code, tape::kClampR);
       aR = div_<T, FAST>((f1 + B2) + sqrt(cl ? T(0) : D), 2 * R[RO]);
-    } else {
-      aR = div_<T, FAST>((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f1 * f2, T(0))), 2 * R[RO]);
     }
     ptR = R[PR] + T(0.5) * B2;
     if (TYPE == FX_LHLLD) {
@@ -307,13 +339,13 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
       f1 = fmin2(T(1), div_<T, FAST>(fmax2(aL1, aR1), fmax2(aL, aR)));
       psi = 2 * sqrt(f1) - f1;
     }
-    f1 = sqrt(decide<TAPE>(aR > aL, code, tape::kArSel) ? aR : aL);  // fmax2(aL, aR)
-    aL = (decide<TAPE>(R[vn] < L[vn], code, tape::kMinR) ? R[vn] : L[vn]) - f1;  // fmin2
-    aR = (decide<TAPE>(R[vn] > L[vn], code, tape::kMaxR) ? R[vn] : L[vn]) + f1;  // fmax2
-    if (decide<TAPE>(aL >= T(0), code, tape::kFL)) {
+    f1 = sqrt(decide<TAPE>(lt_<T, FAST>(aL, aR), code, tape::kArSel) ? aR : aL);  // fmax2(aL, aR)
+    aL = (decide<TAPE>(lt_<T, FAST>(R[vn], L[vn]), code, tape::kMinR) ? R[vn] : L[vn]) - f1;  // fmin2
+    aR = (decide<TAPE>(lt_<T, FAST>(L[vn], R[vn]), code, tape::kMaxR) ? R[vn] : L[vn]) + f1;  // fmax2
+    if (decide<TAPE>(ge0_<T, FAST>(aL), code, tape::kFL)) {
 #pragma unroll
       for (int v = 0; v < NV; ++v) Fo[v] = FL[v];
-    } else if (decide<TAPE>(aR <= T(0), code, tape::kFR)) {
+    } else if (decide<TAPE>(le0_<T, FAST>(aR), code, tape::kFR)) {
 #pragma unroll
       for (int v = 0; v < NV; ++v) Fo[v] = FR[v];
     } else {
@@ -397,13 +429,13 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
         UR1[mt2] = roR * vt2R;
         aL1 = aM - aVL;
         aR1 = aM + aVR;
-        if (decide<TAPE>(aL1 >= T(0), code, tape::kLS)) {  // F(L*) :514-519
+        if (decide<TAPE>(ge0_<T, FAST>(aL1), code, tape::kLS)) {  // F(L*) :514-519
 #pragma unroll
           for (int v = MX; v <= EN; ++v) Fo[v] = aL * (UL1[v] - UL[v]) + FL[v];
           Fo[RO] = aL * (UL1[RO] - L[RO]) + FL[RO];
           Fo[bt1] = aL * (UL1[bt1] - L[bt1]) + FL[bt1];
           Fo[bt2] = aL * (UL1[bt2] - L[bt2]) + FL[bt2];
-        } else if (decide<TAPE>(aR1 <= T(0), code, tape::kRS)) {  // F(R*) :522-527
+        } else if (decide<TAPE>(le0_<T, FAST>(aR1), code, tape::kRS)) {  // F(R*) :522-527
 #pragma unroll
           for (int v = MX; v <= EN; ++v) Fo[v] = aR * (UR1[v] - UR[v]) + FR[v];
           Fo[RO] = aR * (UR1[RO] - R[RO]) + FR[RO];
@@ -419,7 +451,7 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
           const T at2 = f1 * (roLs * vt2L + roRs * vt2R + (UR1[bt2] - UL1[bt2]) * f2);
           U2[bt1] = f1 * (roLs * UR1[bt1] + roRs * UL1[bt1] + roLs * roRs * (vt1R - vt1L) * f2);
           U2[bt2] = f1 * (roLs * UR1[bt2] + roRs * UL1[bt2] + roLs * roRs * (vt2R - vt2L) * f2);
-          if (decide<TAPE>(aM >= T(0), code, tape::kSSLeft)) {  // F(L**)
+          if (decide<TAPE>(ge0_<T, FAST>(aM), code, tape::kSSLeft)) {  // F(L**)
             U2[RO] = roL;
             U2[EN] = UL1[EN] - roLs * (vt1L * UL1[bt1] + vt2L * UL1[bt2] - at1 * U2[bt1] - at2 * U2[bt2]) * f2;
             U2[mn] = roL * aM;
@@ -455,7 +487,8 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
 template <class T, bool FAST = false>
 __device__ __forceinline__ T fast_speed(T f1, T B2, T bd, T ro) {
   const T f2 = 4 * f1 * (bd * bd);
-  return sqrt(div_<T, FAST>((f1 + B2) + sqrt(fmax2((f1 + B2) * (f1 + B2) - f2, T(0))), 2 * ro));
+  const T D = (f1 + B2) * (f1 + B2) - f2;
+  return sqrt(div_<T, FAST>((f1 + B2) + sqrt(lt0_<T, FAST>(D) ? T(0) : D), 2 * ro));
 }
 
 }  // namespace omhd
