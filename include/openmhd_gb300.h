@@ -309,6 +309,25 @@ int omhd_step2d_noalloc(double* U_dev, const omhd_config* cfg, double t0, int ns
 size_t omhd_step2d_noalloc_max_doubles(void);
 
 /* ======================================================================
+ * Snapshot files (2D_basic/fileio.f90:16-115, 3D_basic/fileio.f90:16-122):
+ * the reference's stream layout, native byte order:
+ *   t | ix, jx[, kx] (int32) | x, y[, z] | U: 9 planes (mx..ps) | V: vx vy vz pr
+ * Arrays may be host or device memory.  V may be NULL: it is then computed
+ * from U on the GPU (u2v.f90), and a failing u2v (negative pressure or
+ * density) is returned without writing.  fileio_input reads t, x, y[, z] and
+ * U and rejects a file whose sizes differ (fileio.f90:77-82) with
+ * OMHD_BAD_ARG.  The reference's readers read these files unchanged.
+ * ==================================================================== */
+int omhd_fileio_output(const char* path, int nd, int ix, int jx, int kx, double t, const double* x,
+                       const double* y, const double* z, const double* U, const double* V);
+int omhd_fileio_input(const char* path, int nd, int ix, int jx, int kx, double* t, double* x, double* y,
+                      double* z, double* U);
+/* a solver's state, primitives, coordinates and time to a snapshot file, and
+ * restart from one (put_state with the file's t) */
+int omhd_solver_write(omhd_solver* s, const char* path);
+int omhd_solver_read(omhd_solver* s, const char* path);
+
+/* ======================================================================
  * Reverse mode through time (no counterpart in the reference).  The
  * gradient of a scalar functional J(U_N) with respect to the initial state
  * U_0 of `nsteps` fused FP64 TVD-RK2 steps (2D, HLLD, minmod or MC, GLM,

@@ -122,6 +122,10 @@ SIGNATURES = [
     ("omhd_ensemble_sync", I, [P, C.POINTER(StepInfo)]),
     ("omhd_step2d_noalloc", I, [P, C.POINTER(Config), D, I, P, C.POINTER(StepInfo)]),
     ("omhd_step2d_noalloc_max_doubles", C.c_size_t, []),
+    ("omhd_fileio_output", I, [C.c_char_p, I, I, I, I, D, P, P, P, P, P]),
+    ("omhd_fileio_input", I, [C.c_char_p, I, I, I, I, c_double_p, P, P, P, P]),
+    ("omhd_solver_write", I, [P, C.c_char_p]),
+    ("omhd_solver_read", I, [P, C.c_char_p]),
     ("omhd_adjoint_create", I, [C.POINTER(Config), I, I, C.POINTER(C.c_void_p)]),
     ("omhd_adjoint_destroy", I, [P]),
     ("omhd_adjoint_set_stream", I, [P, P]),

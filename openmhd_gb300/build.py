@@ -35,6 +35,7 @@ UNITS = {
     "omhd_noalloc.cu": [],
     "omhd_ensemble.cu": [],
     "omhd_adjoint.cu": ["--fmad=true"],
+    "omhd_fileio.cu": [],
 }
 
 

@@ -242,6 +242,17 @@ class Solver:
         self.lib.omhd_solver_coords(self._h, x.ctypes.data, y.ctypes.data, z.ctypes.data)
         return x, y, z
 
+    # -- snapshot files (fileio.f90 layout) --
+    def write_snapshot(self, path: str):
+        """State, primitives, coordinates and t in the reference's field file format."""
+        self._check(self.lib.omhd_solver_write(self._h, str(path).encode()))
+        return self
+
+    def read_snapshot(self, path: str):
+        """Restart from a field file (its t becomes the solver's time)."""
+        self._check(self.lib.omhd_solver_read(self._h, str(path).encode()))
+        return self
+
     # -- stepping --
     def step(self, n: int = 1):
         import torch
