@@ -226,8 +226,11 @@ typedef struct {
 
 /* model initial states (reference-style problem setups) */
 typedef struct {
-  int kind;            /* 0 Orszag-Tang (2D_basic/model.f90), 1 KH shear layer, 2 Harris sheet (3D) */
-  double amp;          /* OT: B amplitude scale (1); KH: shear speed; Harris: A_y amplitude */
+  int kind;            /* 0 Orszag-Tang (2D_basic/model.f90), 1 KH shear layer, 2 Harris sheet (3D),
+                          3 2D reconnection (2D_reconnection/model.f90), 4 Brio-Wu (1D_basic/model.f90),
+                          5 3D field loop (3D_basic/model.f90) */
+  double amp;          /* OT: B amplitude scale (1); KH: shear speed; Harris: A_y amplitude;
+                          reconnection: X-point perturbation b1; field loop: A amplitude */
   double bx0;          /* KH: uniform Bx */
   double phase_x, phase_y;  /* OT phase shifts (0, 0) */
   double beta;         /* Harris plasma beta */

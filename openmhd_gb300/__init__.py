@@ -10,11 +10,14 @@ from .solver import (  # noqa: F401
     OmhdError,
     Solver,
     SolverConfig,
+    brio_wu,
+    field_loop3d,
     flip,
     harris3d,
     kelvin_helmholtz,
     orszag_tang,
+    reconnection2d,
 )
 
 __all__ = ["Solver", "SolverConfig", "ModelSpec", "OmhdError", "orszag_tang", "kelvin_helmholtz",
-           "harris3d", "flip"]
+           "harris3d", "reconnection2d", "brio_wu", "field_loop3d", "flip"]

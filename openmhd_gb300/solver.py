@@ -155,6 +155,42 @@ def harris3d(nx: int = 512, ny: int = 256, nz: int = 512, precision: str = "fp64
     return cfg, ModelSpec(kind=2, beta=beta, amp=amp, seed=seed)
 
 
+def reconnection2d(nx: int = 2000, ny: int = 500, precision: str = "fp64", limiter: str = "minmod",
+                   flux: str = "hlld", cfl: float = 0.35, tend: float = 0.0, beta: float = 0.2, b1: float = 0.03):
+    """2D resistive reconnection (2D_reconnection/model.f90, bc.f90, flux_resistive.f90):
+    the quarter domain x in [0,200], y >= 0 with dy = dx, Harris sheet
+    rho = 1 + cosh(y)^-2/beta, Bx = tanh(y) plus an X-point perturbation of
+    amplitude b1, and the reference's symmetry walls (bc_for_U): west/east flip
+    mx, mz, By, psi; south flips my, mz, Bx, psi; north flips my, By."""
+    dx = 200.0 / nx
+    lr = flip(MX, MZ, BY, PS)
+    cfg = SolverConfig(nd=2, ix=nx + 2, jx=ny + 2, dx=dx, dy=dx, x0=0.0, y0=0.0, cfl=cfl, limiter=limiter,
+                       flux=flux, precision=precision, tend=tend, eta="recon2d", bc_kind=(1, 1, 1, 1, 0, 0),
+                       bc_flip=(lr, lr, flip(MY, MZ, BX, PS), flip(MY, BY), 0, 0))
+    return cfg, ModelSpec(kind=3, beta=beta, amp=b1)
+
+
+def brio_wu(nx: int = 300, precision: str = "fp64", limiter: str = "minmod", flux: str = "hlld", cfl: float = 0.8,
+            tend: float = 0.2):
+    """Brio-Wu MHD shock tube (1D_basic/model.f90, the active states) on
+    x in [-0.5, 0.5] with zero-gradient ends, run as a strip of two periodic
+    rows of the 2D step."""
+    dx = 1.0 / nx
+    cfg = SolverConfig(nd=2, ix=nx + 2, jx=4, dx=dx, dy=dx, x0=-0.5, y0=0.0, cfl=cfl, limiter=limiter, flux=flux,
+                       precision=precision, tend=tend, bc_kind=(1, 1, 0, 0, 0, 0), bc_flip=(0,) * 6)
+    return cfg, ModelSpec(kind=4)
+
+
+def field_loop3d(nx: int = 100, ny: int = 100, nz: int = 200, precision: str = "fp64", limiter: str = "minmod",
+                 flux: str = "hlld", cfl: float = 0.3, tend: float = 1.01, amp: float = 0.001):
+    """3D field-loop advection (3D_basic/model.f90): a cylindrical A-profile
+    loop, v = (1, 1, 2), on x in [-0.5, 0.5], y from -0.5, z from -1, periodic."""
+    dx = 1.0 / nx
+    cfg = SolverConfig(nd=3, ix=nx + 2, jx=ny + 2, kx=nz + 2, dx=dx, dy=dx, dz=dx, x0=-0.5, y0=-0.5, z0=-1.0,
+                       cfl=cfl, limiter=limiter, flux=flux, precision=precision, tend=tend)
+    return cfg, ModelSpec(kind=5, amp=amp)
+
+
 # ---------------------------------------------------------------------------
 # solver
 # ---------------------------------------------------------------------------

@@ -894,6 +894,14 @@ static double harris_ay(const omo_model* m, double x, double y, double z, double
   return m->amp * exp(-(z * z) / 4.0) * s;
 }
 
+/* vector-potential profile of the 3D field loop, 3D_basic/model.f90:1-6 (mya3) */
+static double loop_a3(double xx, double yy, double zz) {
+  const double myr = 0.3;
+  const double a = 2 * xx + zz;
+  const double m2 = fmin2(fmin2((a - 2) * (a - 2), a * a), (a + 2) * (a + 2));
+  return fmax2(0.0, myr - sqrt(yy * yy + m2 / 5.0));
+}
+
 void omo_model_fill(const omo_model* m, double* U, const double* x, const double* y,
                     const double* z, int ix, int jx, int kx, double dx, double dy, double dz) {
   const size_t n = (size_t)ix * jx * kx;
@@ -925,7 +933,7 @@ void omo_model_fill(const omo_model* m, double* U, const double* x, const double
           bx = m->bx0;
           by = 0.0;
           bz = 0.0;
-        } else {
+        } else if (m->kind == 2) {
           /* Harris sheet in z: Bx=tanh(z), rho=1+cosh(z)^-2/beta, p=0.5*beta*rho, v=0,
            * plus curl(A_y yhat) by centred half-cell differences (3D_basic/model.f90:61-63) */
           const double Lx = dx * (ix - 2), Ly = dy * (jx - 2);
@@ -940,6 +948,37 @@ void omo_model_fill(const omo_model* m, double* U, const double* x, const double
           bx = tanh(z[k]) - dAz;
           by = 0.0;
           bz = dAx;
+        } else if (m->kind == 3) {
+          /* 2D reconnection, 2D_reconnection/model.f90:37-58 (b1 = amp) */
+          const double chy = cosh(fmin2(y[j], 25.0));
+          ro = 1.0 + (1.0 / (chy * chy)) / m->beta;
+          pr = 0.5 * m->beta * ro;
+          vx = 0.0; vy = 0.0; vz = 0.0;
+          const double r2 = x[i] * x[i] + y[j] * y[j];
+          bx = tanh(y[j]) - m->amp * y[j] * exp(-r2 / 4.0);
+          by = 0.0 + m->amp * x[i] * exp(-r2 / 4.0);
+          bz = 0.0;
+        } else if (m->kind == 4) {
+          /* Brio-Wu shock tube, 1D_basic/model.f90:43-68 (the active states) */
+          const int left = x[i] < 0.0;
+          ro = left ? 1.0 : 0.125;
+          pr = left ? 1.0 : 0.1;
+          vx = 0.0; vy = 0.0; vz = 0.0;
+          bx = 0.75;
+          by = left ? 1.0 : -1.0;
+          bz = 0.0;
+        } else {
+          /* 3D field loop, 3D_basic/model.f90:37-66 (A amplitude = amp) */
+          ro = 1.0;
+          pr = 1.0;
+          vx = 1.0; vy = 1.0; vz = 2.0;
+          const double fx = -(m->amp / dx) * (1.0 / sqrt(5.0));
+          const double fz = +(m->amp / dx) * (2.0 / sqrt(5.0));
+          const double h = dx / 2;
+          const double xx = x[i], yy = y[j], zz = z[k];
+          bx = fz * (loop_a3(xx, yy + h, zz) - loop_a3(xx, yy - h, zz));
+          by = fx * (loop_a3(xx, yy, zz + h) - loop_a3(xx, yy, zz - h)) - fz * (loop_a3(xx + h, yy, zz) - loop_a3(xx - h, yy, zz));
+          bz = -fx * (loop_a3(xx, yy + h, zz) - loop_a3(xx, yy - h, zz));
         }
         const double v2 = vx * vx + vy * vy + vz * vz;
         const double B2 = bx * bx + by * by + bz * bz;

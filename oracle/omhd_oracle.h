@@ -115,7 +115,8 @@ double omo_uniform_pm1(uint64_t seed, uint64_t n);
 
 /* models: fill x,y,z and U (all cells incl. ghosts), then the caller applies bc. */
 typedef struct {
-  int kind;            /* 0 Orszag-Tang, 1 KH shear layer (zero-gradient y), 2 Harris sheet 3D */
+  int kind;            /* 0 Orszag-Tang, 1 KH shear layer (zero-gradient y), 2 Harris sheet 3D,
+                          3 2D reconnection, 4 Brio-Wu, 5 3D field loop */
   double amp;          /* OT: B amplitude scale; KH: shear speed; Harris: perturbation amplitude */
   double bx0;          /* KH: guide Bx */
   double phase_x, phase_y;  /* OT phase shifts */

@@ -212,3 +212,44 @@ def test_3d_periodic_multichunk_vs_oracle(cuda_lib, oracle_mod):
     s.sync()
     g.step(2)
     _cmp(s, g, 1e-12, "3d periodic")
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64_parity", 1e-12), ("fp64", 1e-10)])
+def test_reconnection2d_symmetry_walls_vs_oracle(cuda_lib, oracle_mod, precision, tol):
+    """2D_reconnection: Harris sheet + X-point perturbation, resistive, all four
+    walls with the reference's sign flips (2D_reconnection/bc.f90:6-50)."""
+    from openmhd_gb300 import reconnection2d
+
+    cfg, model = reconnection2d(96, 32, precision=precision)
+    s, g = _pair(cfg, model, oracle_mod)
+    s.step(6)
+    s.sync()
+    g.step(6)
+    _cmp(s, g, tol, "reconnection2d")
+
+
+def test_brio_wu_to_tend_vs_oracle(cuda_lib, oracle_mod):
+    """Brio-Wu shock tube run to t = 0.2 as in 1D_basic/main.f90 (cfl 0.8):
+    same step count, states within the N-step tolerance."""
+    from openmhd_gb300 import brio_wu
+
+    cfg, model = brio_wu(200, precision="fp64")
+    s, g = _pair(cfg, model, oracle_mod)
+    info = s.run_until(cfg.tend)
+    g.run_until(cfg.tend)
+    assert info.steps == g.steps and abs(info.t - g.t) <= 1e-12
+    _cmp(s, g, 1e-9, "brio-wu")
+    U = s.get_state_numpy()
+    assert np.array_equal(U[:, 1, :], U[:, 2, :])  # the strip stays one-dimensional
+
+
+def test_field_loop3d_vs_oracle(cuda_lib, oracle_mod):
+    """3D_basic field-loop advection, all periodic (3D_basic/bc.f90)."""
+    from openmhd_gb300 import field_loop3d
+
+    cfg, model = field_loop3d(24, 20, 40, precision="fp64")
+    s, g = _pair(cfg, model, oracle_mod)
+    s.step(4)
+    s.sync()
+    g.step(4)
+    _cmp(s, g, 1e-10, "field loop")

@@ -162,3 +162,32 @@ def test_3d_axis_rotation_symmetry(oracle_mod):
     h.step(2)
     back = h.U[[1, 2, 0, 3, 4, 6, 7, 5, 8]].transpose(0, 3, 1, 2)
     assert np.abs(g.U - back).max() < 1e-12
+
+
+def test_more_problem_setups(oracle_mod):
+    """Initial states of the 2D reconnection, Brio-Wu and 3D field-loop setups
+    (2D_reconnection/model.f90, 1D_basic/model.f90, 3D_basic/model.f90)."""
+    import math
+
+    from openmhd_gb300 import brio_wu, field_loop3d, reconnection2d
+
+    cfg, m = brio_wu(40)
+    g = oracle_mod.Grid.from_solver_config(cfg).model(m.kind)
+    left, right = g.x < 0, g.x >= 0
+    assert np.all(g.U[4][:, left] == 1.0) and np.all(g.U[4][:, right] == 0.125)
+    assert np.all(g.U[6][:, left] == 1.0) and np.all(g.U[6][:, right] == -1.0) and np.all(g.U[5] == 0.75)
+    assert np.allclose(g.U[3][:, left], 0.5 * (0.75**2 + 1) + 1.0 / (5.0 / 3.0 - 1))
+
+    cfg, m = reconnection2d(64, 24)
+    g = oracle_mod.Grid.from_solver_config(cfg).model(m.kind, amp=m.amp, beta=m.beta)
+    j = 20
+    y = g.y[j]
+    assert np.allclose(g.U[4][j, 1:-1], 1 + 1 / math.cosh(y) ** 2 / 0.2)
+    far = g.x[1:-1] > 30
+    assert np.allclose(g.U[5][j, 1:-1][far], math.tanh(y)) and np.all(g.U[0:3] == 0.0)
+
+    cfg, m = field_loop3d(16, 16, 32)
+    g = oracle_mod.Grid.from_solver_config(cfg).model(m.kind, amp=m.amp)
+    assert np.all(g.U[0] == 1.0) and np.all(g.U[1] == 1.0) and np.all(g.U[2] == 2.0)
+    Bmag = np.sqrt((g.U[5:8] ** 2).sum(axis=0))
+    assert 5e-4 < Bmag.max() < 5e-3 and np.mean(Bmag == 0.0) > 0.5  # a loop in a field-free box
