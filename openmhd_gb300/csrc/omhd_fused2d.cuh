@@ -195,14 +195,16 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
       const int cx = xd ? q % XS : qq % TX, cy = xd ? q / XS : qq / TX;
       const int gi = xd ? gi0 - 1 + cx : gi0 + cx, gj = xd ? gj0 + cy : gj0 - 1 + cy;
       const bool own = (xd ? (cx >= 1 && cx <= TX) : (cy >= 1 && cy <= TY)) && gi <= ix - 2 && gj <= jx - 2;
-      const size_t tc = (size_t)tape_cell(gi, ix, perx) + (size_t)ix * tape_cell(gj, jx, pery);
-      unsigned char* tl = a.tlim + (size_t)(xd ? 0 : 1) * NV * N;
+      const size_t tc = (TAPE == tape::kReplay || a.tlim)
+                            ? (size_t)tape_cell(gi, ix, perx) + (size_t)ix * tape_cell(gj, jx, pery)
+                            : 0;
+      unsigned char* tl = a.tlim ? a.tlim + (size_t)(xd ? 0 : 1) * NV * N : nullptr;
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
         double l, r;
         unsigned char k = (TAPE == tape::kReplay) ? tl[v * N + tc] : 0;
         reconstruct_fp64<OMHD_FAST, TAPE>(lm, W[v * PL + o - st], W[v * PL + o], W[v * PL + o + st], l, r, &k);
-        if (TAPE == tape::kRecord && own) tl[v * N + tc] = k;
+        if (TAPE == tape::kRecord && own && tl) tl[v * N + tc] = k;
         dl[v * (xd ? NXS : NYS) + qq] = l;
         dr[v * (xd ? NXS : NYS) + qq] = r;
       }
@@ -260,7 +262,7 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
         const size_t tc = (size_t)(gl < 0 ? 0 : (gl > ix - 2 ? ix - 2 : gl)) + (size_t)ix * (gj > jx - 2 ? jx - 2 : gj);
         unsigned k = (TAPE == tape::kReplay) ? a.tface[tc] : 0u;
         riemann_flux<T, 1, FLUX, OMHD_FAST, TAPE>(L, R, ch, gam, r1, r2, Fo, &k);
-        if (TAPE == tape::kRecord && (fx >= 1 || gi0 == 1) && gl <= ix - 2 && gj <= jx - 2)
+        if (TAPE == tape::kRecord && a.tface && (fx >= 1 || gi0 == 1) && gl <= ix - 2 && gj <= jx - 2)
           a.tface[tc] = (unsigned short)k;
       }
       if (resist) {  // 2D_reconnection/flux_resistive.f90:266-283
@@ -296,7 +298,7 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
         const size_t tc = (size_t)(gi > ix - 2 ? ix - 2 : gi) + (size_t)ix * (gl < 0 ? 0 : (gl > jx - 2 ? jx - 2 : gl));
         unsigned k = (TAPE == tape::kReplay) ? a.tface[N + tc] : 0u;
         riemann_flux<T, 2, FLUX, OMHD_FAST, TAPE>(L, R, ch, gam, r1, r2, Fo, &k);
-        if (TAPE == tape::kRecord && (fy >= 1 || gj0 == 1) && gl <= jx - 2 && gi <= ix - 2)
+        if (TAPE == tape::kRecord && a.tface && (fy >= 1 || gj0 == 1) && gl <= jx - 2 && gi <= ix - 2)
           a.tface[N + tc] = (unsigned short)k;
       }
       if (resist) {  // 2D_reconnection/flux_resistive.f90:289-306

@@ -5,7 +5,18 @@
 #include "omhd_fused2d.cuh"
 
 namespace omhd {
-int launch_stage2d_fp64(const StageArgs& a, cudaStream_t s) { return v_fp64::launch_variant<double>(a, s); }
+// HLLD with minmod or MC runs the tape-recording instantiation with recording
+// switched off (null tape pointers): one machine code for the plain and the
+// recording step, so a recorded run reproduces a plain run bit for bit.
+int launch_stage2d_fp64(const StageArgs& a, cudaStream_t s) {
+  if (a.flux_type == FX_HLLD && (a.lm_type == LM_MINMOD || a.lm_type == LM_MC)) {
+    StageArgs b = a;
+    b.tlim = nullptr;
+    b.tface = nullptr;
+    return v_fp64::launch_one<double, FX_HLLD, tape::kRecord>(b, s);
+  }
+  return v_fp64::launch_variant<double>(a, s);
+}
 int launch_stage2d_fp64_tape(const StageArgs& a, int mode, cudaStream_t s) {
   if (a.flux_type != FX_HLLD || a.nd != 2 || !a.tlim || !a.tface) return (int)cudaErrorInvalidValue;
   if (a.lm_type != LM_MINMOD && a.lm_type != LM_MC) return (int)cudaErrorInvalidValue;

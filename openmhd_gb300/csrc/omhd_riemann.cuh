@@ -63,6 +63,12 @@ __device__ __forceinline__ T div_(T a, T b) {
   if constexpr (FAST && sizeof(T) == 8) return a * rcp_nr(b);
   return a / b;
 }
+// a / b given rb = rcp_<T,FAST>(b) computed once for several numerators
+template <class T, bool FAST>
+__device__ __forceinline__ T divr_(T a, T b, T rb) {
+  if constexpr (FAST && sizeof(T) == 8) return a * rb;
+  return a / b;
+}
 
 enum { LM_FLAT = 0, LM_MINMOD = 1, LM_MC = 2, LM_VANLEER = 3, LM_KOREN = 4 };
 enum { FX_LLF = 0, FX_HLL = 1, FX_HLLC = 2, FX_HLLD = 3, FX_LHLLD = 4 };
@@ -203,8 +209,12 @@ __device__ __forceinline__ void reconstruct_t(int type, T wm, T w0, T wp, T& lef
 // from it (tape::kArSel ... tape::kClampR); the arithmetic is unchanged.
 template <class T, int DIR, int TYPE, bool FAST = false, int TAPE = tape::kNone>
 __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV], T ch, T gamma, T r1,
-                                             T r2, T (&Fo)[NV], unsigned* code = nullptr) {
+                                             T r2, T (&Fo)[NV], unsigned* code_io = nullptr) {
   using tape::decide;
+  // the face's decision word lives in a register here; read from / written to
+  // *code_io once (replay / record)
+  unsigned code_reg = (TAPE == tape::kReplay) ? *code_io : 0u;
+  unsigned* const code = &code_reg;
   constexpr int vn = VX + (DIR - 1) % 3, vt1 = VX + DIR % 3, vt2 = VX + (DIR + 1) % 3;
   constexpr int bn = BX + (DIR - 1) % 3, bt1 = BX + DIR % 3, bt2 = BX + (DIR + 1) % 3;
   constexpr int mn = MX + (DIR - 1) % 3, mt1 = MX + DIR % 3, mt2 = MX + (DIR + 1) % 3;
@@ -364,8 +374,11 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
       } else {
         pt = ptL + L[RO] * (aL - L[vn]) * (aM - L[vn]);
       }
-      const T roL = div_<T, FAST>(L[RO] * (aL - L[vn]), aL - aM);
-      const T roR = div_<T, FAST>(R[RO] * (aR - R[vn]), aR - aM);
+      // one reciprocal of (aL - aM) and of (aR - aM) serves rho*, E* (FAST)
+      const T ieL = (FAST && sizeof(T) == 8) ? rcp_<T, FAST>(aL - aM) : T(0);
+      const T ieR = (FAST && sizeof(T) == 8) ? rcp_<T, FAST>(aR - aM) : T(0);
+      const T roL = divr_<T, FAST>(L[RO] * (aL - L[vn]), aL - aM, ieL);
+      const T roR = divr_<T, FAST>(R[RO] * (aR - R[vn]), aR - aM, ieR);
       // Alfven speeds; the FAST variant keeps 1/sqrt(rho*) for the central states
       T rsL = T(0), rsR = T(0);
       if constexpr (FAST && sizeof(T) == 8) {
@@ -377,7 +390,8 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
       const T aBn = (TAPE == tape::kNone) ? fabs(Uh[bn]) : (bneg ? -Uh[bn] : Uh[bn]);
       const T aVL = (FAST && sizeof(T) == 8) ? aBn * rsL : aBn / sqrt(roL);
       const T aVR = (FAST && sizeof(T) == 8) ? aBn * rsR : aBn / sqrt(roR);
-      if (TYPE == FX_HLLD && decide<TAPE>((aL >= (aM - hllg_factor * aVL)) || ((aM + hllg_factor * aVR) >= aR),
+      if (TYPE == FX_HLLD && decide<TAPE>(!lt_<T, FAST>(aL, aM - hllg_factor * aVL) ||
+                                              !lt_<T, FAST>(aM + hllg_factor * aVR, aR),
                                           code, tape::kG)) {
         // HLLC-G fallback :450-476
         f2 = aL * aR;
@@ -385,10 +399,10 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
         Fo[bt2] = f1 * (aR * FL[bt2] - aL * FR[bt2] + f2 * (R[bt2] - L[bt2]));
         const T at1 = div_<T, FAST>(Uh[mt1], Uh[RO]);
         const T at2 = div_<T, FAST>(Uh[mt2], Uh[RO]);
-        const T enL = div_<T, FAST>(((aL - L[vn]) * UL[EN] - ptL * L[vn] + pt * aM +
-                       Uh[bn] * (vBL - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])), (aL - aM));
-        const T enR = div_<T, FAST>(((aR - R[vn]) * UR[EN] - ptR * R[vn] + pt * aM +
-                       Uh[bn] * (vBR - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])), (aR - aM));
+        const T enL = divr_<T, FAST>(((aL - L[vn]) * UL[EN] - ptL * L[vn] + pt * aM +
+                       Uh[bn] * (vBL - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])), (aL - aM), ieL);
+        const T enR = divr_<T, FAST>(((aR - R[vn]) * UR[EN] - ptR * R[vn] + pt * aM +
+                       Uh[bn] * (vBR - aM * Uh[bn] - at1 * Uh[bt1] - at2 * Uh[bt2])), (aR - aM), ieR);
         if constexpr (TAPE != tape::kNone)
           f1 = decide<TAPE>(signbit(aM) == 0, code, tape::kGLeft) ? T(1) : T(0);  // 0.5 + sign(0.5, aM)
         else
@@ -400,42 +414,50 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
         Fo[EN] = f1 * (aL * (enL - UL[EN]) + FL[EN]) + f2 * (aR * (enR - UR[EN]) + FR[EN]);
         Fo[RO] = f1 * (aL * (roL - L[RO]) + FL[RO]) + f2 * (aR * (roR - R[RO]) + FR[RO]);
       } else {
-        T UL1[NV], UR1[NV];
-        // L* (:482-493)
-        const T tL = aL - L[vn];
-        f1 = rcp_<T, FAST>(L[RO] * tL * (aL - aM) - Uh[bn] * Uh[bn]);
-        UL1[bt1] = L[bt1] * f1 * (L[RO] * (tL * tL) - Uh[bn] * Uh[bn]);
-        UL1[bt2] = L[bt2] * f1 * (L[RO] * (tL * tL) - Uh[bn] * Uh[bn]);
-        const T vt1L = L[vt1] - f1 * Uh[bn] * L[bt1] * (aM - L[vn]);
-        const T vt2L = L[vt2] - f1 * Uh[bn] * L[bt2] * (aM - L[vn]);
-        UL1[RO] = roL;
-        UL1[EN] = div_<T, FAST>(((aL - L[vn]) * UL[EN] - ptL * L[vn] + pt * aM +
-                   Uh[bn] * (vBL - aM * Uh[bn] - vt1L * UL1[bt1] - vt2L * UL1[bt2])), (aL - aM));
-        UL1[mn] = roL * aM;
-        UL1[mt1] = roL * vt1L;
-        UL1[mt2] = roL * vt2L;
-        // R* (:496-507)
-        const T tR = aR - R[vn];
-        f1 = rcp_<T, FAST>(R[RO] * tR * (aR - aM) - Uh[bn] * Uh[bn]);
-        UR1[bt1] = R[bt1] * f1 * (R[RO] * (tR * tR) - Uh[bn] * Uh[bn]);
-        UR1[bt2] = R[bt2] * f1 * (R[RO] * (tR * tR) - Uh[bn] * Uh[bn]);
-        const T vt1R = R[vt1] - f1 * Uh[bn] * R[bt1] * (aM - R[vn]);
-        const T vt2R = R[vt2] - f1 * Uh[bn] * R[bt2] * (aM - R[vn]);
-        UR1[RO] = roR;
-        UR1[EN] = div_<T, FAST>(((aR - R[vn]) * UR[EN] - ptR * R[vn] + pt * aM +
-                   Uh[bn] * (vBR - aM * Uh[bn] - vt1R * UR1[bt1] - vt2R * UR1[bt2])), (aR - aM));
-        UR1[mn] = roR * aM;
-        UR1[mt1] = roR * vt1R;
-        UR1[mt2] = roR * vt2R;
+        // Region first (aL1, aR1 need only aM and the Alfven speeds), then the
+        // intermediate states that region uses: F(L*) needs L* only, F(R*)
+        // R* only, the central states both.  Same expressions as :482-507.
         aL1 = aM - aVL;
         aR1 = aM + aVR;
-        if (decide<TAPE>(ge0_<T, FAST>(aL1), code, tape::kLS)) {  // F(L*) :514-519
+        const bool sLs = decide<TAPE>(ge0_<T, FAST>(aL1), code, tape::kLS);
+        const bool sRs = !sLs && decide<TAPE>(le0_<T, FAST>(aR1), code, tape::kRS);
+        T UL1[NV] = {}, UR1[NV] = {};
+        T vt1L = T(0), vt2L = T(0), vt1R = T(0), vt2R = T(0);
+        if (!sRs) {  // L* (:482-493)
+          const T tL = aL - L[vn];
+          f1 = rcp_<T, FAST>(L[RO] * tL * (aL - aM) - Uh[bn] * Uh[bn]);
+          UL1[bt1] = L[bt1] * f1 * (L[RO] * (tL * tL) - Uh[bn] * Uh[bn]);
+          UL1[bt2] = L[bt2] * f1 * (L[RO] * (tL * tL) - Uh[bn] * Uh[bn]);
+          vt1L = L[vt1] - f1 * Uh[bn] * L[bt1] * (aM - L[vn]);
+          vt2L = L[vt2] - f1 * Uh[bn] * L[bt2] * (aM - L[vn]);
+          UL1[RO] = roL;
+          UL1[EN] = divr_<T, FAST>(((aL - L[vn]) * UL[EN] - ptL * L[vn] + pt * aM +
+                     Uh[bn] * (vBL - aM * Uh[bn] - vt1L * UL1[bt1] - vt2L * UL1[bt2])), (aL - aM), ieL);
+          UL1[mn] = roL * aM;
+          UL1[mt1] = roL * vt1L;
+          UL1[mt2] = roL * vt2L;
+        }
+        if (!sLs) {  // R* (:496-507)
+          const T tR = aR - R[vn];
+          f1 = rcp_<T, FAST>(R[RO] * tR * (aR - aM) - Uh[bn] * Uh[bn]);
+          UR1[bt1] = R[bt1] * f1 * (R[RO] * (tR * tR) - Uh[bn] * Uh[bn]);
+          UR1[bt2] = R[bt2] * f1 * (R[RO] * (tR * tR) - Uh[bn] * Uh[bn]);
+          vt1R = R[vt1] - f1 * Uh[bn] * R[bt1] * (aM - R[vn]);
+          vt2R = R[vt2] - f1 * Uh[bn] * R[bt2] * (aM - R[vn]);
+          UR1[RO] = roR;
+          UR1[EN] = divr_<T, FAST>(((aR - R[vn]) * UR[EN] - ptR * R[vn] + pt * aM +
+                     Uh[bn] * (vBR - aM * Uh[bn] - vt1R * UR1[bt1] - vt2R * UR1[bt2])), (aR - aM), ieR);
+          UR1[mn] = roR * aM;
+          UR1[mt1] = roR * vt1R;
+          UR1[mt2] = roR * vt2R;
+        }
+        if (sLs) {  // F(L*) :514-519
 #pragma unroll
           for (int v = MX; v <= EN; ++v) Fo[v] = aL * (UL1[v] - UL[v]) + FL[v];
           Fo[RO] = aL * (UL1[RO] - L[RO]) + FL[RO];
           Fo[bt1] = aL * (UL1[bt1] - L[bt1]) + FL[bt1];
           Fo[bt2] = aL * (UL1[bt2] - L[bt2]) + FL[bt2];
-        } else if (decide<TAPE>(le0_<T, FAST>(aR1), code, tape::kRS)) {  // F(R*) :522-527
+        } else if (sRs) {  // F(R*) :522-527
 #pragma unroll
           for (int v = MX; v <= EN; ++v) Fo[v] = aR * (UR1[v] - UR[v]) + FR[v];
           Fo[RO] = aR * (UR1[RO] - R[RO]) + FR[RO];
@@ -481,6 +503,7 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   // GLM fluxes :580-581
   Fo[bn] = T(0.5) * ((L[PS] + R[PS]) - ch * (R[bn] - L[bn]));
   Fo[PS] = T(0.5) * (ch2 * (L[bn] + R[bn]) - ch * (R[PS] - L[PS]));
+  if constexpr (TAPE == tape::kRecord) *code_io = code_reg;
 }
 
 // Fast magnetosonic speed used by set_dt (2D_basic/set_dt.f90:27-34).
