@@ -287,7 +287,7 @@ def run_ours(args):
         "peak_source": "DFMA throughput measured in this run (omhd_probe_fp64_peak); "
                        "MEASURED_PEAKS.json has no FP64 entry",
         "flops_per_cell_update": flops_cu,
-        "kernel": "omhd::v_fp64::k_stage2d<double,HLLD>",
+        "kernel": "omhd::v_fp64::k_stage2d<double,HLLD,tape-capable>",
         "hbm": {"achieved": hbm_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                 "frac": hbm_gbs / peaks.get("hbm_gbs", 1.0), "peak_source": peak_src,
                 "bytes_per_cell_update": BYTES_PER_CELL_UPDATE_2D},

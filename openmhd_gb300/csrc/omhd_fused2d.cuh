@@ -52,7 +52,7 @@ struct Geo2 {
     return sizeof(T) * (size_t)NV * (RY * RX + 2 * (NXS + NYS) + NXF + NYF);
   }
 };
-using GeoDefault = Geo2<32, 8>;
+using GeoDefault = Geo2<16, 16>;
 
 __device__ __forceinline__ int map_index(int g, int n, bool periodic) {
   if (g >= 0 && g < n) return g;
