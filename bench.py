@@ -284,8 +284,9 @@ def run_ours(args):
         "bound": "fp64", "achieved": ach_tflops, "peak": fp64_peak / 1e3, "unit": "TFLOP/s",
         "frac": ach_tflops / (fp64_peak / 1e3),
         "traffic": _load_traffic("stage2d_fp64_kh4096x2048.md"),
-        "peak_source": "DFMA throughput measured in this run (omhd_probe_fp64_peak); "
-                       "MEASURED_PEAKS.json has no FP64 entry",
+        "peak_source": "DFMA burst throughput measured in this run (omhd_probe_fp64_peak: register "
+                       "operands, best of five launches; nominal 1.25 TFLOP/s); MEASURED_PEAKS.json has no "
+                       "FP64 entry",
         "flops_per_cell_update": flops_cu,
         "kernel": "omhd::v_fp64::k_stage2d<double,HLLD,tape-capable>",
         "hbm": {"achieved": hbm_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
@@ -631,6 +632,42 @@ def run_profile(args):
     return 0 if info.status == 0 else 1
 
 
+def run_profile_adjoint(args):
+    """Small fixed adjoint run for profiler captures: KH --nx x --ny, --steps
+    steps (checkpoint every step), one forward and one backward."""
+    import torch
+
+    from openmhd_gb300 import Solver, kelvin_helmholtz
+    from openmhd_gb300.adjoint import AdjointRun
+
+    cfg, model = kelvin_helmholtz(args.nx, args.ny, precision="fp64")
+    base = Solver(cfg).init_model(model).U.clone()
+    run = AdjointRun(cfg, args.steps, 1)
+    UN = run.forward(base)
+    g = torch.zeros_like(UN)
+    g[6] = 2 * UN[6]
+    gU0 = run.backward(g)
+    run.sync()
+    print(json.dumps({"profile": "adjoint", "nx": args.nx, "ny": args.ny, "steps": args.steps,
+                      "grad_norm": float(gU0.norm())}), flush=True)
+    return 0
+
+
+def run_profile_batched(args):
+    """Small fixed ensemble run for profiler captures: 16 members, sides
+    {256..512}, FP32-mixed, --steps steps with the 32x8 tiling, 2 CTAs/SM."""
+    from openmhd_gb300.ensemble import Ensemble, batched_problem_set
+
+    cfgs, models = batched_problem_set(16, seed=1, precision="mixed", sides=[256, 320, 384, 448, 512])
+    ens = Ensemble(cfgs).init_models(models)
+    ens.set_tiling(0, 2)
+    ens.step(args.steps)
+    infos = ens.sync()
+    print(json.dumps({"profile": "batched", "members": len(cfgs), "cells": ens.cells, "steps": args.steps,
+                      "status": max(i.status for i in infos)}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -643,15 +680,21 @@ def main():
     ap.add_argument("--no-3d", action="store_true")
     ap.add_argument("--adjoint-only", action="store_true", help="run the adjoint leg alone")
     ap.add_argument("--profile", action="store_true", help="small fixed run for profiler captures")
+    ap.add_argument("--profile-adjoint", action="store_true", help="small adjoint run for profiler captures")
+    ap.add_argument("--profile-batched", action="store_true", help="small ensemble run for profiler captures")
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--nz", type=int, default=0)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_parity", "mixed"])
     args = ap.parse_args()
-    if args.profile:
+    if args.profile or args.profile_adjoint or args.profile_batched:
         from openmhd_gb300.build import build
 
         build()
+        if args.profile_adjoint:
+            return run_profile_adjoint(args)
+        if args.profile_batched:
+            return run_profile_batched(args)
         return run_profile(args)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

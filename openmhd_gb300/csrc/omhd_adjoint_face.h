@@ -351,38 +351,54 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
       }
     } else {
       // ---- HLLD (flux_solver.f90:482-572) ----
-      // L* and R* intermediate states
-      const double dL = L[kRO] * tL * eL - Ubn * Ubn, iL = arcp(dL);
-      const double kL = L[kRO] * (tL * tL) - Ubn * Ubn;
-      const double UL1bt1 = L[bt1] * iL * kL, UL1bt2 = L[bt2] * iL * kL;
-      const double dmL = aM - L[vn];
-      const double vt1L = L[vt1] - iL * Ubn * L[bt1] * dmL, vt2L = L[vt2] - iL * Ubn * L[bt2] * dmL;
-      const double QL = sL.vB - aM * Ubn - vt1L * UL1bt1 - vt2L * UL1bt2;
-      const double numL = tL * sL.UE - sL.pt * L[vn] + pts * aM + Ubn * QL;
-      const double UL1E = numL * ieL;
-      double UL1m[3];
-      UL1m[mn] = roL * aM;
-      UL1m[mt1] = roL * vt1L;
-      UL1m[mt2] = roL * vt2L;
-      const double dR = R[kRO] * tR * eR - Ubn * Ubn, iR = arcp(dR);
-      const double kR = R[kRO] * (tR * tR) - Ubn * Ubn;
-      const double UR1bt1 = R[bt1] * iR * kR, UR1bt2 = R[bt2] * iR * kR;
-      const double dmR = aM - R[vn];
-      const double vt1R = R[vt1] - iR * Ubn * R[bt1] * dmR, vt2R = R[vt2] - iR * Ubn * R[bt2] * dmR;
-      const double QR = sR.vB - aM * Ubn - vt1R * UR1bt1 - vt2R * UR1bt2;
-      const double numR = tR * sR.UE - sR.pt * R[vn] + pts * aM + Ubn * QR;
-      const double UR1E = numR * ieR;
-      double UR1m[3];
-      UR1m[mn] = roR * aM;
-      UR1m[mt1] = roR * vt1R;
-      UR1m[mt2] = roR * vt2R;
+      // Region first (it needs only aM and the Alfven speeds), then the
+      // intermediate states it uses: F(L*) needs L* only, F(R*) R* only,
+      // the central states both (the forward kernel does the same).
       const double aL1 = aM - aVL, aR1 = aM + aVR;
+      const bool sLs = decide<MODE>(aL1 >= 0.0, code, tape::kLS);
+      const bool sRs = !sLs && decide<MODE>(aR1 <= 0.0, code, tape::kRS);
+      double dL = 0, iL = 0, kL = 0, UL1bt1 = 0, UL1bt2 = 0, dmL = 0, vt1L = 0, vt2L = 0, QL = 0, UL1E = 0;
+      double UL1m[3] = {0, 0, 0};
+      if (!sRs) {  // L* (flux_solver.f90:482-493)
+        dL = L[kRO] * tL * eL - Ubn * Ubn;
+        iL = arcp(dL);
+        kL = L[kRO] * (tL * tL) - Ubn * Ubn;
+        UL1bt1 = L[bt1] * iL * kL;
+        UL1bt2 = L[bt2] * iL * kL;
+        dmL = aM - L[vn];
+        vt1L = L[vt1] - iL * Ubn * L[bt1] * dmL;
+        vt2L = L[vt2] - iL * Ubn * L[bt2] * dmL;
+        QL = sL.vB - aM * Ubn - vt1L * UL1bt1 - vt2L * UL1bt2;
+        const double numL = tL * sL.UE - sL.pt * L[vn] + pts * aM + Ubn * QL;
+        UL1E = numL * ieL;
+        UL1m[mn] = roL * aM;
+        UL1m[mt1] = roL * vt1L;
+        UL1m[mt2] = roL * vt2L;
+      }
+      double dR = 0, iR = 0, kR = 0, UR1bt1 = 0, UR1bt2 = 0, dmR = 0, vt1R = 0, vt2R = 0, QR = 0, UR1E = 0;
+      double UR1m[3] = {0, 0, 0};
+      if (!sLs) {  // R* (flux_solver.f90:496-507)
+        dR = R[kRO] * tR * eR - Ubn * Ubn;
+        iR = arcp(dR);
+        kR = R[kRO] * (tR * tR) - Ubn * Ubn;
+        UR1bt1 = R[bt1] * iR * kR;
+        UR1bt2 = R[bt2] * iR * kR;
+        dmR = aM - R[vn];
+        vt1R = R[vt1] - iR * Ubn * R[bt1] * dmR;
+        vt2R = R[vt2] - iR * Ubn * R[bt2] * dmR;
+        QR = sR.vB - aM * Ubn - vt1R * UR1bt1 - vt2R * UR1bt2;
+        const double numR = tR * sR.UE - sR.pt * R[vn] + pts * aM + Ubn * QR;
+        UR1E = numR * ieR;
+        UR1m[mn] = roR * aM;
+        UR1m[mt1] = roR * vt1R;
+        UR1m[mt2] = roR * vt2R;
+      }
 
       double gUL1m[3] = {0, 0, 0}, gUR1m[3] = {0, 0, 0};
       double gUL1E = 0, gUR1E = 0, gUL1bt1 = 0, gUL1bt2 = 0, gUR1bt1 = 0, gUR1bt2 = 0;
       double gvt1L = 0, gvt2L = 0, gvt1R = 0, gvt2R = 0;
 
-      if (decide<MODE>(aL1 >= 0.0, code, tape::kLS)) {  // F(L*)
+      if (sLs) {  // F(L*)
         for (int k = 0; k < 3; ++k) {
           gSL += gF[k] * (UL1m[k] - sL.Um[k]);
           gUL1m[k] += SL * gF[k];
@@ -399,7 +415,7 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
         gUL1bt2 += SL * gF[bt2];
         gL[bt2] -= SL * gF[bt2];
         for (int q = 0; q < 7; ++q) gsL.F[fl[q]] += gF[fl[q]];
-      } else if (decide<MODE>(aR1 <= 0.0, code, tape::kRS)) {  // F(R*)
+      } else if (sRs) {  // F(R*)
         for (int k = 0; k < 3; ++k) {
           gSR += gF[k] * (UR1m[k] - sR.Um[k]);
           gUR1m[k] += SR * gF[k];
@@ -567,7 +583,7 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
         gsqR += grRs;
       }
       // ---- back through the L* and R* states ----
-      {  // L
+      if (!sRs) {  // L
         groL += gUL1m[mn] * aM + gUL1m[mt1] * vt1L + gUL1m[mt2] * vt2L;
         gaM += gUL1m[mn] * roL;
         gvt1L += gUL1m[mt1] * roL;
@@ -623,7 +639,7 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
         geL += gdL * L[kRO] * tL;
         gUh[bn] -= 2 * gdL * Ubn;
       }
-      {  // R
+      if (!sLs) {  // R
         groR += gUR1m[mn] * aM + gUR1m[mt1] * vt1R + gUR1m[mt2] * vt2R;
         gaM += gUR1m[mn] * roR;
         gvt1R += gUR1m[mt1] * roR;

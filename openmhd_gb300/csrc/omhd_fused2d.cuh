@@ -52,7 +52,17 @@ struct Geo2 {
     return sizeof(T) * (size_t)NV * (RY * RX + 2 * (NXS + NYS) + NXF + NYF);
   }
 };
-using GeoDefault = Geo2<16, 16>;
+// tile of the single-grid stage kernel per arithmetic type: the FP64 kernel is
+// FP64-pipe bound and gains from the smaller halo of 16x16 tiles; the
+// FP32-mixed kernel (two CTAs per SM) runs faster on 32x8
+template <class T>
+struct GeoFor {
+  using type = Geo2<16, 16>;
+};
+template <>
+struct GeoFor<float> {
+  using type = Geo2<32, 8>;
+};
 
 __device__ __forceinline__ int map_index(int g, int n, bool periodic) {
   if (g >= 0 && g < n) return g;
@@ -388,7 +398,8 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
 
 // one CTA per tile of one grid
 template <class T, int FLUX, int TAPE = tape::kNone>
-__global__ void __launch_bounds__(GeoDefault::NT) k_stage2d(const StageArgs a) {
+__global__ void __launch_bounds__(GeoFor<T>::type::NT) k_stage2d(const StageArgs a) {
+  using G = typename GeoFor<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red32[32];
   __shared__ int skip;
@@ -398,7 +409,7 @@ __global__ void __launch_bounds__(GeoDefault::NT) k_stage2d(const StageArgs a) {
   if (threadIdx.x == 0) skip = st->done || *(volatile int*)&a.err->code;
   __syncthreads();
   if (skip) return;
-  const double vcell = stage2d_tile<T, FLUX, GeoDefault, TAPE>(a, blockIdx.x, blockIdx.y, smem_raw, st->dt, st->ch,
+  const double vcell = stage2d_tile<T, FLUX, G, TAPE>(a, blockIdx.x, blockIdx.y, smem_raw, st->dt, st->ch,
                                                                st->glm_f);
   if (a.stage == 2) {
     const double bm = block_max_pos(vcell, red32);
@@ -458,7 +469,8 @@ __global__ void __launch_bounds__(G::NT) k_batch2d(const StageArgs* __restrict__
 
 template <class T, int FLUX, int TAPE = tape::kNone>
 int launch_one(const StageArgs& a, cudaStream_t s) {
-  const size_t bytes = GeoDefault::smem_bytes<T>();
+  using G = typename GeoFor<T>::type;
+  const size_t bytes = G::template smem_bytes<T>();
   static bool configured = false;
   if (!configured) {
     cudaError_t e =
@@ -466,8 +478,8 @@ int launch_one(const StageArgs& a, cudaStream_t s) {
     if (e != cudaSuccess) return (int)e;
     configured = true;
   }
-  dim3 grid((a.ix - 2 + GeoDefault::TX - 1) / GeoDefault::TX, (a.jx - 2 + GeoDefault::TY - 1) / GeoDefault::TY);
-  k_stage2d<T, FLUX, TAPE><<<grid, GeoDefault::NT, bytes, s>>>(a);
+  dim3 grid((a.ix - 2 + G::TX - 1) / G::TX, (a.jx - 2 + G::TY - 1) / G::TY);
+  k_stage2d<T, FLUX, TAPE><<<grid, G::NT, bytes, s>>>(a);
   return (int)cudaGetLastError();
 }
 

@@ -421,9 +421,12 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
         aR1 = aM + aVR;
         const bool sLs = decide<TAPE>(ge0_<T, FAST>(aL1), code, tape::kLS);
         const bool sRs = !sLs && decide<TAPE>(le0_<T, FAST>(aR1), code, tape::kRS);
+        // (the FP32 arithmetic of the mixed variant computes both states
+        // unconditionally: there the branch costs more than the work)
+        constexpr bool kEager = !(FAST && sizeof(T) == 8);
         T UL1[NV] = {}, UR1[NV] = {};
         T vt1L = T(0), vt2L = T(0), vt1R = T(0), vt2R = T(0);
-        if (!sRs) {  // L* (:482-493)
+        if (kEager || !sRs) {  // L* (:482-493)
           const T tL = aL - L[vn];
           f1 = rcp_<T, FAST>(L[RO] * tL * (aL - aM) - Uh[bn] * Uh[bn]);
           UL1[bt1] = L[bt1] * f1 * (L[RO] * (tL * tL) - Uh[bn] * Uh[bn]);
@@ -437,7 +440,7 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
           UL1[mt1] = roL * vt1L;
           UL1[mt2] = roL * vt2L;
         }
-        if (!sLs) {  // R* (:496-507)
+        if (kEager || !sLs) {  // R* (:496-507)
           const T tR = aR - R[vn];
           f1 = rcp_<T, FAST>(R[RO] * tR * (aR - aM) - Uh[bn] * Uh[bn]);
           UR1[bt1] = R[bt1] * f1 * (R[RO] * (tR * tR) - Uh[bn] * Uh[bn]);
