@@ -47,10 +47,13 @@ struct Geo2 {
   static constexpr int NXFP = round32(NXF);       // x faces padded to whole warps
   // one thread per y face (or padded x face), at least one per cell
   static constexpr int NT = imax(imax(NXFP, round32(NYF)), round32(TX * TY));
+  // face states in T, face fluxes in FP64 (the flux differences are FP64,
+  // so each flux is widened once, when it is stored)
   template <class T>
   static constexpr size_t smem_bytes() {
-    return sizeof(T) * (size_t)NV * (RY * RX + 2 * (NXS + NYS) + NXF + NYF);
+    return sizeof(T) * (size_t)NV * (RY * RX + 2 * (NXS + NYS)) + sizeof(double) * (size_t)NV * (NXF + NYF);
   }
+  static_assert((NV * (RY * RX + 2 * (NXS + NYS))) % 2 == 0, "flux block must start 8-byte aligned");
 };
 // tile of the single-grid stage kernel per arithmetic type: the FP64 kernel is
 // FP64-pipe bound and gains from the smaller halo of 16x16 tiles; the
@@ -114,8 +117,8 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
   T* SRx = SLx + NV * NXS;                // [NV][NXS] lower x-face states of cells
   T* SLy = SRx + NV * NXS;                // [NV][NYS]
   T* SRy = SLy + NV * NYS;                // [NV][NYS]
-  T* FBx = SRy + NV * NYS;                // [NV][NXF] x-face fluxes
-  T* FBy = FBx + NV * NXF;                // [NV][NYF] y-face fluxes
+  double* FBx = reinterpret_cast<double*>(SRy + NV * NYS);  // [NV][NXF] x-face fluxes
+  double* FBy = FBx + NV * NXF;                              // [NV][NYF] y-face fluxes
 
   const int ix = a.ix, jx = a.jx;
   const size_t N = (size_t)ix * jx;
@@ -291,7 +294,7 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
         }
       }
 #pragma unroll
-      for (int v = 0; v < NV; ++v) FBx[v * NXF + q] = Fo[v];
+      for (int v = 0; v < NV; ++v) FBx[v * NXF + q] = double(Fo[v]);
     } else {
       const int qq = q - NXFP;
       const int cx = qq % TX, fy = qq / TX;
@@ -327,7 +330,7 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
         }
       }
 #pragma unroll
-      for (int v = 0; v < NV; ++v) FBy[v * NYF + qq] = Fo[v];
+      for (int v = 0; v < NV; ++v) FBy[v * NYF + qq] = double(Fo[v]);
     }
   }
   __syncthreads();
@@ -344,8 +347,8 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
         // F(i-1/2) - F(i+1/2) in FP64
-        const double dF = double(FBx[v * NXF + ty * XF + tx]) - double(FBx[v * NXF + ty * XF + tx + 1]);
-        const double gm = double(FBy[v * NYF + ty * TX + tx]), gp = double(FBy[v * NYF + (ty + 1) * TX + tx]);
+        const double dF = FBx[v * NXF + ty * XF + tx] - FBx[v * NXF + ty * XF + tx + 1];
+        const double gm = FBy[v * NYF + ty * TX + tx], gp = FBy[v * NYF + (ty + 1) * TX + tx];
         double d;
         if (a.iso)
           d = dtx * (dF + gm - gp);  // rk.f90:26-35 operation order
