@@ -351,6 +351,7 @@ struct omhd_adjoint {
   double* lam[3] = {nullptr, nullptr, nullptr};
   size_t bytes = 0;
   bool have_forward = false, have_tape = false;
+  bool last_seg_live = false;  // the plain forward left the last segment's stage inputs and tape in place
   omhd_error_info last = {};
 };
 
@@ -455,11 +456,23 @@ int run_forward(omhd_adjoint* a, const double* U0, double* UN, int mode) {
       k_log_step<<<1, 1, 0, a->stream>>>(s->st, a->logd + 3 * (size_t)k);
     r = acerr(a, cudaGetLastError(), "step record kernel");
     if (r) break;
-    if (mode == tape::kNone)
+    const int klast = (a->nck - 1) * a->every;  // first step of the last segment
+    if (mode == tape::kNone && k >= klast) {
+      // the last segment is reversed first: keep its stage inputs and decisions
+      // now, so the backward pass need not recompute it
+      const int j = k - klast;
+      r = acerr(a, cudaMemcpyAsync(a->segU + S * j, a->Uw, sizeof(double) * S, cudaMemcpyDeviceToDevice, a->stream),
+                "segment copy");
+      r = r ? r : omhd_solver_bind(s, a->Uw, a->segU1 + S * j);
+      r = r ? r : taped_step(a, tape::kRecord, a->segTl + 2 * tl_stride(a) * j, a->segTf + 2 * tf_stride(a) * j);
+    } else if (mode == tape::kNone) {
       r = omhd_solver_step(s, 1);
-    else
+    } else {
       r = taped_step(a, mode, a->fullTl + 2 * tl_stride(a) * k, a->fullTf + 2 * tf_stride(a) * k);
+    }
   }
+  const int rb = omhd_solver_bind(s, a->Uw, a->U1w);
+  r = r ? r : rb;
   if (!r && UN)
     r = acerr(a, cudaMemcpyAsync(UN, a->Uw, sizeof(double) * S, cudaMemcpyDeviceToDevice, a->stream), "state copy");
   return r;
@@ -546,9 +559,9 @@ int omhd_adjoint_set_stream(omhd_adjoint* a, void* stream) {
 
 int omhd_adjoint_forward(omhd_adjoint* a, const double* U0, double* UN) {
   if (!a || !U0) return OMHD_BAD_ARG;
-  a->have_forward = false;
+  a->have_forward = a->last_seg_live = false;
   const int r = run_forward(a, U0, UN, tape::kNone);
-  if (!r) a->have_forward = true;
+  if (!r) a->have_forward = a->last_seg_live = true;
   return r;
 }
 
@@ -565,7 +578,7 @@ int omhd_adjoint_record(omhd_adjoint* a, const double* U0, double* UN) {
                   "tape clear");
     if (r) return r;
   }
-  a->have_forward = a->have_tape = false;
+  a->have_forward = a->have_tape = a->last_seg_live = false;
   r = run_forward(a, U0, UN, tape::kRecord);
   r = r ? r
         : acerr(a, cudaMemcpyAsync(a->tlog, a->logd, sizeof(double) * 3 * a->nsteps, cudaMemcpyDeviceToDevice,
@@ -599,12 +612,17 @@ int omhd_adjoint_backward(omhd_adjoint* a, const double* gUN, double* gU0) {
     const int k0 = q * a->every;
     const int k1 = (k0 + a->every < a->nsteps) ? k0 + a->every : a->nsteps;
     // recompute the segment from its checkpoint, keeping each step's stage
-    // inputs and recording its decisions
-    r = acerr(a, cudaMemcpyAsync(a->Uw, a->ck + S * q, sizeof(double) * S, cudaMemcpyDeviceToDevice, a->stream),
-              "checkpoint restore");
-    r = r ? r : acerr(a, cudaMemcpyAsync(s->st, a->ckst + q, sizeof(StepState), cudaMemcpyDeviceToDevice, a->stream),
-                      "checkpoint record restore");
-    for (int k = k0; k < k1 && !r; ++k) {
+    // inputs and recording its decisions (the last segment is still in place
+    // after a plain forward run)
+    const bool live = (q == a->nck - 1) && a->last_seg_live;
+    if (!live) {
+      r = acerr(a, cudaMemcpyAsync(a->Uw, a->ck + S * q, sizeof(double) * S, cudaMemcpyDeviceToDevice, a->stream),
+                "checkpoint restore");
+      r = r ? r
+            : acerr(a, cudaMemcpyAsync(s->st, a->ckst + q, sizeof(StepState), cudaMemcpyDeviceToDevice, a->stream),
+                    "checkpoint record restore");
+    }
+    for (int k = k0; k < k1 && !r && !live; ++k) {
       const int j = k - k0;
       double* Uk = a->segU + S * j;
       r = acerr(a, cudaMemcpyAsync(Uk, a->Uw, sizeof(double) * S, cudaMemcpyDeviceToDevice, a->stream), "segment copy");
@@ -625,6 +643,7 @@ int omhd_adjoint_backward(omhd_adjoint* a, const double* gUN, double* gU0) {
     k_adj_final<<<ceil_div((long long)a->n, 256), 256, 0, a->stream>>>(a->geo, lcur, gU0);
     r = acerr(a, cudaGetLastError(), "adjoint final kernel");
   }
+  if (a->nck > 1) a->last_seg_live = false;  // earlier segments now occupy the buffers
   const int rb = omhd_solver_bind(s, a->Uw, a->U1w);
   return r ? r : rb;
 }
