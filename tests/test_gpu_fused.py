@@ -2,7 +2,7 @@
 step) against the CPU oracle's restatement of the reference driver loop
 (2D_basic/main.f90:56-188) from the same initial state.
 
-Tolerances (the benchmark spec): FP64 path within 1e-12 relative L1 per variable after
+Tolerances: FP64 path within 1e-12 relative L1 per variable after
 one step and 1e-9 after N steps; the no-contraction parity build is compared
 at 1e-13 (its only departure from the oracle's op sequence is the device exp()
 in the GLM factor); the FP32-mixed path within 1e-6 L1 of FP64.  The L1 error
