@@ -81,8 +81,9 @@ __device__ __forceinline__ void load_plane(const StageArgs& a, T* W, int slot, i
     const double* U = a.Uin;
     const double ro = U[RO * N + c];
     const double mx = U[MX * N + c], my = U[MY * N + c], mz = U[MZ * N + c];
-    const double vx = div_<double, OMHD_FAST>(mx, ro), vy = div_<double, OMHD_FAST>(my, ro),
-                 vz = div_<double, OMHD_FAST>(mz, ro);  // 3D_basic/u2v.f90:24
+    const double iro = rcp_<double, OMHD_FAST>(ro);  // one reciprocal for the three velocities
+    const double vx = divr_<double, OMHD_FAST>(mx, ro, iro), vy = divr_<double, OMHD_FAST>(my, ro, iro),
+                 vz = divr_<double, OMHD_FAST>(mz, ro, iro);  // 3D_basic/u2v.f90:24
     const double rv2 = vx * mx + vy * my + vz * mz;
     const double bx = U[BX * N + c], by = U[BY * N + c], bz = U[BZ * N + c];
     const double B2 = bx * bx + by * by + bz * bz;
@@ -406,7 +407,8 @@ __global__ void __launch_bounds__(NT) k_stage3d(const StageArgs a) {
           }
       if (a.stage == 2) {  // 3D_basic/set_dt.f90:27-43 on the new state
         const double ro = out[RO];
-        const double vx = div_<double, OMHD_FAST>(out[MX], ro), vy = div_<double, OMHD_FAST>(out[MY], ro), vz = div_<double, OMHD_FAST>(out[MZ], ro);
+        const double iro = rcp_<double, OMHD_FAST>(ro);  // one reciprocal for the three velocities
+        const double vx = divr_<double, OMHD_FAST>(out[MX], ro, iro), vy = divr_<double, OMHD_FAST>(out[MY], ro, iro), vz = divr_<double, OMHD_FAST>(out[MZ], ro, iro);
         const double rv2 = vx * out[MX] + vy * out[MY] + vz * out[MZ];
         const double B2 = out[BX] * out[BX] + out[BY] * out[BY] + out[BZ] * out[BZ];
         const double pr = f1g * (out[EN] - 0.5 * (rv2 + B2));

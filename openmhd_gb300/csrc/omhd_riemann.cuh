@@ -63,13 +63,23 @@ __device__ __forceinline__ T div_(T a, T b) {
   if constexpr (FAST && sizeof(T) == 8) return a * rcp_nr(b);
   return a / b;
 }
-// square root under the variant's policy: x * (1/sqrt(x)) from rsqrt_nr for
-// FAST FP64 (6 FP64-pipe operations instead of ~10 for the IEEE sqrt; within
-// ~2 ulp), sqrt(+-0) = +-0 kept
+// square root under the variant's policy: sqrt_nr for FAST FP64 (5 FP64-pipe
+// operations instead of ~7 for the IEEE sqrt; within ~1 ulp; IEEE outside the
+// positive normal range, so sqrt(+-0) = +-0)
 template <class T, bool FAST>
 __device__ __forceinline__ T sqrt_(T x) {
-  if constexpr (FAST && sizeof(T) == 8) return (__double_as_longlong(double(x)) > 0) ? x * rsqrt_nr(x) : x;
+  if constexpr (FAST && sizeof(T) == 8) return sqrt_nr(x);
   return sqrt(x);
+}
+// sqrt(a / b) for a, b > 0: a * (1/sqrt(a*b)) for FAST FP64 (one product and
+// one rsqrt refinement replace a division and a square root), IEEE otherwise
+template <class T, bool FAST>
+__device__ __forceinline__ T sqrt_ratio_(T a, T b) {
+  if constexpr (FAST && sizeof(T) == 8) {
+    const double ab = a * b;
+    return pos_normal(ab) ? a * rsqrt_nr(ab) : sqrt(a / b);
+  }
+  return sqrt(a / b);
 }
 // a / b given rb = rcp_<T,FAST>(b) computed once for several numerators
 template <class T, bool FAST>
@@ -228,6 +238,12 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   constexpr int mn = MX + (DIR - 1) % 3, mt1 = MX + DIR % 3, mt2 = MX + (DIR + 1) % 3;
   const T hllg_factor = T(1.001);
   const T ch2 = ch * ch;
+  // FAST FP64 forms of HLLD (fewer FP64-pipe operations, same mathematics):
+  // the fast speeds compared by cross-multiplication and the larger taken as
+  // sqrt(num / (2 rho)) in one rsqrt refinement; a*U - F formed once per side
+  // for the HLL average and the intermediate-state fluxes
+  constexpr bool kF64 = FAST && sizeof(T) == 8;
+  constexpr bool kRatio = kF64 && TYPE == FX_HLLD;
 
   T UL[4], UR[4], FL[NV], FR[NV];
 #pragma unroll
@@ -261,7 +277,8 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
     {  // fmax2(D, 0)
       const T D = (f1 + B2) * (f1 + B2) - f1 * f2;
       const bool cl = decide<TAPE>(lt0_<T, FAST>(D), code, tape::kClampL);
-      aL = div_<T, FAST>((f1 + B2) + sqrt(cl ? T(0) : D), 2 * L[RO]);
+      const T num = (f1 + B2) + sqrt_<T, FAST>(cl ? T(0) : D);
+      aL = kRatio ? num : div_<T, FAST>(num, 2 * L[RO]);  // kRatio: numerator of cf^2
     }
     ptL = L[PR] + T(0.5) * B2;
     if (TYPE == FX_LHLLD) {
@@ -293,7 +310,8 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
     {  // fmax2(D, 0)
       const T D = (f1 + B2) * (f1 + B2) - f1 * f2;
       const bool cl = decide<TAPE>(lt0_<T, FAST>(D), code, tape::kClampR);
-      aR = div_<T, FAST>((f1 + B2) + sqrt(cl ? T(0) : D), 2 * R[RO]);
+      const T num = (f1 + B2) + sqrt_<T, FAST>(cl ? T(0) : D);
+      aR = kRatio ? num : div_<T, FAST>(num, 2 * R[RO]);  // kRatio: numerator of cf^2
     }
     ptR = R[PR] + T(0.5) * B2;
     if (TYPE == FX_LHLLD) {
@@ -357,7 +375,12 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
       f1 = fmin2(T(1), div_<T, FAST>(fmax2(aL1, aR1), fmax2(aL, aR)));
       psi = 2 * sqrt(f1) - f1;
     }
-    f1 = sqrt(decide<TAPE>(lt_<T, FAST>(aL, aR), code, tape::kArSel) ? aR : aL);  // fmax2(aL, aR)
+    if constexpr (kRatio) {  // cf^2 = num / (2 rho): numL/rhoL < numR/rhoR <=> numL*rhoR < numR*rhoL
+      const bool sr = decide<TAPE>(lt_<T, FAST>(aL * R[RO], aR * L[RO]), code, tape::kArSel);
+      f1 = sqrt_ratio_<T, FAST>(sr ? aR : aL, 2 * (sr ? R[RO] : L[RO]));
+    } else {
+      f1 = sqrt_<T, FAST>(decide<TAPE>(lt_<T, FAST>(aL, aR), code, tape::kArSel) ? aR : aL);  // fmax2(aL, aR)
+    }
     aL = (decide<TAPE>(lt_<T, FAST>(R[vn], L[vn]), code, tape::kMinR) ? R[vn] : L[vn]) - f1;  // fmin2
     aR = (decide<TAPE>(lt_<T, FAST>(L[vn], R[vn]), code, tape::kMaxR) ? R[vn] : L[vn]) + f1;  // fmax2
     if (decide<TAPE>(ge0_<T, FAST>(aL), code, tape::kFL)) {
@@ -367,12 +390,28 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
 #pragma unroll
       for (int v = 0; v < NV; ++v) Fo[v] = FR[v];
     } else {
-      T Uh[NV];
+      T Uh[NV], gL[NV] = {}, gR[NV] = {};
       f1 = rcp_<T, FAST>(aR - aL);
+      if constexpr (kF64) {  // g = a*U - F per side (MX..BZ)
 #pragma unroll
-      for (int v = MX; v <= MZ; ++v) Uh[v] = f1 * (aR * UR[v] - aL * UL[v] - FR[v] + FL[v]);
+        for (int v = MX; v <= EN; ++v) {
+          gL[v] = aL * UL[v] - FL[v];
+          gR[v] = aR * UR[v] - FR[v];
+        }
 #pragma unroll
-      for (int v = RO; v <= BZ; ++v) Uh[v] = f1 * (aR * R[v] - aL * L[v] - FR[v] + FL[v]);
+        for (int v = RO; v <= BZ; ++v) {
+          gL[v] = aL * L[v] - FL[v];
+          gR[v] = aR * R[v] - FR[v];
+        }
+#pragma unroll
+        for (int v = MX; v <= BZ; ++v)
+          if (v != EN) Uh[v] = f1 * (gR[v] - gL[v]);
+      } else {
+#pragma unroll
+        for (int v = MX; v <= MZ; ++v) Uh[v] = f1 * (aR * UR[v] - aL * UL[v] - FR[v] + FL[v]);
+#pragma unroll
+        for (int v = RO; v <= BZ; ++v) Uh[v] = f1 * (aR * R[v] - aL * L[v] - FR[v] + FL[v]);
+      }
       const T aM = div_<T, FAST>(Uh[mn], Uh[RO]);
       T pt;
       if (TYPE == FX_LHLLD) {
@@ -463,17 +502,33 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
           UR1[mt2] = roR * vt2R;
         }
         if (sLs) {  // F(L*) :514-519
+          if constexpr (kF64) {  // aL*(UL1 - UL) + FL = aL*UL1 - gL
 #pragma unroll
-          for (int v = MX; v <= EN; ++v) Fo[v] = aL * (UL1[v] - UL[v]) + FL[v];
-          Fo[RO] = aL * (UL1[RO] - L[RO]) + FL[RO];
-          Fo[bt1] = aL * (UL1[bt1] - L[bt1]) + FL[bt1];
-          Fo[bt2] = aL * (UL1[bt2] - L[bt2]) + FL[bt2];
+            for (int v = MX; v <= EN; ++v) Fo[v] = aL * UL1[v] - gL[v];
+            Fo[RO] = aL * UL1[RO] - gL[RO];
+            Fo[bt1] = aL * UL1[bt1] - gL[bt1];
+            Fo[bt2] = aL * UL1[bt2] - gL[bt2];
+          } else {
+#pragma unroll
+            for (int v = MX; v <= EN; ++v) Fo[v] = aL * (UL1[v] - UL[v]) + FL[v];
+            Fo[RO] = aL * (UL1[RO] - L[RO]) + FL[RO];
+            Fo[bt1] = aL * (UL1[bt1] - L[bt1]) + FL[bt1];
+            Fo[bt2] = aL * (UL1[bt2] - L[bt2]) + FL[bt2];
+          }
         } else if (sRs) {  // F(R*) :522-527
+          if constexpr (kF64) {
 #pragma unroll
-          for (int v = MX; v <= EN; ++v) Fo[v] = aR * (UR1[v] - UR[v]) + FR[v];
-          Fo[RO] = aR * (UR1[RO] - R[RO]) + FR[RO];
-          Fo[bt1] = aR * (UR1[bt1] - R[bt1]) + FR[bt1];
-          Fo[bt2] = aR * (UR1[bt2] - R[bt2]) + FR[bt2];
+            for (int v = MX; v <= EN; ++v) Fo[v] = aR * UR1[v] - gR[v];
+            Fo[RO] = aR * UR1[RO] - gR[RO];
+            Fo[bt1] = aR * UR1[bt1] - gR[bt1];
+            Fo[bt2] = aR * UR1[bt2] - gR[bt2];
+          } else {
+#pragma unroll
+            for (int v = MX; v <= EN; ++v) Fo[v] = aR * (UR1[v] - UR[v]) + FR[v];
+            Fo[RO] = aR * (UR1[RO] - R[RO]) + FR[RO];
+            Fo[bt1] = aR * (UR1[bt1] - R[bt1]) + FR[bt1];
+            Fo[bt2] = aR * (UR1[bt2] - R[bt2]) + FR[bt2];
+          }
         } else {  // central states :533-572
           T U2[NV];
           const T roLs = (FAST && sizeof(T) == 8) ? roL * rsL : sqrt(roL);
@@ -490,22 +545,38 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
             U2[mn] = roL * aM;
             U2[mt1] = roL * at1;
             U2[mt2] = roL * at2;
+            if constexpr (kF64) {
 #pragma unroll
-            for (int v = MX; v <= EN; ++v) Fo[v] = aL1 * U2[v] - (aL1 - aL) * UL1[v] - aL * UL[v] + FL[v];
-            Fo[RO] = aL1 * U2[RO] - (aL1 - aL) * UL1[RO] - aL * L[RO] + FL[RO];
-            Fo[bt1] = aL1 * U2[bt1] - (aL1 - aL) * UL1[bt1] - aL * L[bt1] + FL[bt1];
-            Fo[bt2] = aL1 * U2[bt2] - (aL1 - aL) * UL1[bt2] - aL * L[bt2] + FL[bt2];
+              for (int v = MX; v <= EN; ++v) Fo[v] = aL1 * U2[v] - (aL1 - aL) * UL1[v] - gL[v];
+              Fo[RO] = aL1 * U2[RO] - (aL1 - aL) * UL1[RO] - gL[RO];
+              Fo[bt1] = aL1 * U2[bt1] - (aL1 - aL) * UL1[bt1] - gL[bt1];
+              Fo[bt2] = aL1 * U2[bt2] - (aL1 - aL) * UL1[bt2] - gL[bt2];
+            } else {
+#pragma unroll
+              for (int v = MX; v <= EN; ++v) Fo[v] = aL1 * U2[v] - (aL1 - aL) * UL1[v] - aL * UL[v] + FL[v];
+              Fo[RO] = aL1 * U2[RO] - (aL1 - aL) * UL1[RO] - aL * L[RO] + FL[RO];
+              Fo[bt1] = aL1 * U2[bt1] - (aL1 - aL) * UL1[bt1] - aL * L[bt1] + FL[bt1];
+              Fo[bt2] = aL1 * U2[bt2] - (aL1 - aL) * UL1[bt2] - aL * L[bt2] + FL[bt2];
+            }
           } else {  // F(R**)
             U2[RO] = roR;
             U2[EN] = UR1[EN] + roRs * (vt1R * UR1[bt1] + vt2R * UR1[bt2] - at1 * U2[bt1] - at2 * U2[bt2]) * f2;
             U2[mn] = roR * aM;
             U2[mt1] = roR * at1;
             U2[mt2] = roR * at2;
+            if constexpr (kF64) {
 #pragma unroll
-            for (int v = MX; v <= EN; ++v) Fo[v] = aR1 * U2[v] - (aR1 - aR) * UR1[v] - aR * UR[v] + FR[v];
-            Fo[RO] = aR1 * U2[RO] - (aR1 - aR) * UR1[RO] - aR * R[RO] + FR[RO];
-            Fo[bt1] = aR1 * U2[bt1] - (aR1 - aR) * UR1[bt1] - aR * R[bt1] + FR[bt1];
-            Fo[bt2] = aR1 * U2[bt2] - (aR1 - aR) * UR1[bt2] - aR * R[bt2] + FR[bt2];
+              for (int v = MX; v <= EN; ++v) Fo[v] = aR1 * U2[v] - (aR1 - aR) * UR1[v] - gR[v];
+              Fo[RO] = aR1 * U2[RO] - (aR1 - aR) * UR1[RO] - gR[RO];
+              Fo[bt1] = aR1 * U2[bt1] - (aR1 - aR) * UR1[bt1] - gR[bt1];
+              Fo[bt2] = aR1 * U2[bt2] - (aR1 - aR) * UR1[bt2] - gR[bt2];
+            } else {
+#pragma unroll
+              for (int v = MX; v <= EN; ++v) Fo[v] = aR1 * U2[v] - (aR1 - aR) * UR1[v] - aR * UR[v] + FR[v];
+              Fo[RO] = aR1 * U2[RO] - (aR1 - aR) * UR1[RO] - aR * R[RO] + FR[RO];
+              Fo[bt1] = aR1 * U2[bt1] - (aR1 - aR) * UR1[bt1] - aR * R[bt1] + FR[bt1];
+              Fo[bt2] = aR1 * U2[bt2] - (aR1 - aR) * UR1[bt2] - aR * R[bt2] + FR[bt2];
+            }
           }
         }
       }
@@ -522,7 +593,7 @@ template <class T, bool FAST = false>
 __device__ __forceinline__ T fast_speed(T f1, T B2, T bd, T ro) {
   const T f2 = 4 * f1 * (bd * bd);
   const T D = (f1 + B2) * (f1 + B2) - f2;
-  return sqrt_<T, FAST>(div_<T, FAST>((f1 + B2) + sqrt_<T, FAST>(lt0_<T, FAST>(D) ? T(0) : D), 2 * ro));
+  return sqrt_ratio_<T, FAST>((f1 + B2) + sqrt_<T, FAST>(lt0_<T, FAST>(D) ? T(0) : D), 2 * ro);
 }
 
 }  // namespace omhd
