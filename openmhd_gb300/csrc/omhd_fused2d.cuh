@@ -90,9 +90,6 @@ __device__ __forceinline__ double eta_at(int kind, double x, double y, double z)
   return 0.0;
 }
 
-// One stage on one tile (tile coordinates bxi, byi) of the grid described by
-// `a`; returns this thread's CFL speed of the updated cell (stage 2) or 0.
-// All threads of the CTA must call it (it synchronises the CTA).
 // canonical interior cell of a (possibly ghost or out-of-grid) index along an
 // axis of extent n, for decision-tape lookups: periodic ghosts wrap, other
 // indices clamp (their states are unused)
@@ -106,34 +103,48 @@ __device__ __forceinline__ int tape_cell(int g, int n, bool periodic) {
   return g < 1 ? 1 : (g > n - 2 ? n - 2 : g);
 }
 
-template <class T, int FLUX, class G, int TAPE = tape::kNone>
-__device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int byi, unsigned char* smem_raw,
-                                               double dt, double chd, double glmf) {
-  constexpr int TX = G::TX, TY = G::TY, NT = G::NT, RX = G::RX, RY = G::RY;
-  constexpr int NXS = G::NXS, NYS = G::NYS, NXF = G::NXF, NYF = G::NYF, NXFP = G::NXFP;
-  constexpr int PL = RX * RY;
-  T* W = reinterpret_cast<T*>(smem_raw);  // [NV][RY][RX] primitive halo tile
-  T* SLx = W + NV * PL;                   // [NV][NXS] upper x-face states of cells
-  T* SRx = SLx + NV * NXS;                // [NV][NXS] lower x-face states of cells
-  T* SLy = SRx + NV * NXS;                // [NV][NYS]
-  T* SRy = SLy + NV * NYS;                // [NV][NYS]
-  double* FBx = reinterpret_cast<double*>(SRy + NV * NYS);  // [NV][NXF] x-face fluxes
-  double* FBy = FBx + NV * NXF;                              // [NV][NYF] y-face fluxes
+// Shared-memory views of one tile: the primitive halo tile W, the face states
+// of both directions, and where the face fluxes go.  Fluxes either have their
+// own FP64 block (FX[v*fxv + cy*(TX+1) + fx], FY[v*fyv + fy*TX + cx]) or, in
+// the FP64 pipelined kernel, overwrite the lower-cell face state that only
+// their own face reads (FX = SLx with fxv = NXS and row stride TX+2).
+template <class T>
+struct TileMem {
+  T* W;
+  T *SLx, *SRx, *SLy, *SRy;
+  double *FX, *FY;
+  int fxv, fxr, fyv;
+};
 
+template <class T, class G>
+__device__ __forceinline__ TileMem<T> tile_mem_separate(unsigned char* smem_raw) {
+  TileMem<T> m;
+  m.W = reinterpret_cast<T*>(smem_raw);
+  m.SLx = m.W + NV * G::RX * G::RY;
+  m.SRx = m.SLx + NV * G::NXS;
+  m.SLy = m.SRx + NV * G::NXS;
+  m.SRy = m.SLy + NV * G::NYS;
+  m.FX = reinterpret_cast<double*>(m.SRy + NV * G::NYS);
+  m.FY = m.FX + NV * G::NXF;
+  m.fxv = G::NXF;
+  m.fxr = G::TX + 1;
+  m.fyv = G::NYF;
+  return m;
+}
+
+// phase A: halo tile load + u2v (+ first GLM half in stage 1); threads t of n
+template <class T, class G>
+__device__ __forceinline__ void phase_load(const StageArgs& a, int bxi, int byi, const TileMem<T>& m, int t, int n,
+                                           double glmf) {
+  constexpr int TX = G::TX, TY = G::TY, RX = G::RX, RY = G::RY, PL = RX * RY;
   const int ix = a.ix, jx = a.jx;
   const size_t N = (size_t)ix * jx;
-  const int tid = threadIdx.x;
   const int gi0 = 1 + bxi * TX, gj0 = 1 + byi * TY;
   const bool perx = a.bc_kind[0] == OMHD_BC_PERIODIC, pery = a.bc_kind[2] == OMHD_BC_PERIODIC;
   const bool resist = a.eta_kind != OMHD_ETA_NONE;
-  const double gamma = a.gamma;
-  const double f1g = gamma - 1;  // u2v.f90:11
-  const T ch = T(chd), gam = T(gamma);
-  const T r1 = T(1.0 / (gamma - 1.0)), r2 = T(gamma / (gamma - 1.0));
-  const int lm = a.lm_type;
-
-  // ---- A: halo tile load + u2v (+ first GLM half in stage 1) ----
-  for (int q = tid; q < PL; q += NT) {
+  const double f1g = a.gamma - 1;  // u2v.f90:11
+  T* W = m.W;
+  for (int q = t; q < PL; q += n) {
     const int rx = q % RX, ry = q / RX;
     const bool cx_in = rx >= 2 && rx < TX + 2, cy_in = ry >= 2 && ry < TY + 2;
     if (!cx_in && !cy_in) {
@@ -170,12 +181,21 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
         raise_error(a.err, OMHD_NEG_DENSITY, gi + 1, gj + 1, 0, 0, ro);
     }
   }
-  __syncthreads();
+}
 
-  // ---- B: slopes in x (cells rx = 1..TX+2 on tile rows) and y (rows
-  //      ry = 1..TY+2 on tile columns) ----
-  constexpr int XS = TX + 2;
-  for (int q = tid; q < NXS + NYS; q += NT) {
+// phase B: slopes in x (cells rx = 1..TX+2 on tile rows) and y (rows
+// ry = 1..TY+2 on tile columns) -> face states of both directions
+template <class T, class G, int TAPE>
+__device__ __forceinline__ void phase_recon(const StageArgs& a, int bxi, int byi, const TileMem<T>& m, int t, int n) {
+  constexpr int TX = G::TX, TY = G::TY, RX = G::RX, RY = G::RY, PL = RX * RY;
+  constexpr int NXS = G::NXS, NYS = G::NYS, XS = TX + 2;
+  const int ix = a.ix, jx = a.jx;
+  const size_t N = (size_t)ix * jx;
+  const int gi0 = 1 + bxi * TX, gj0 = 1 + byi * TY;
+  const bool perx = a.bc_kind[0] == OMHD_BC_PERIODIC, pery = a.bc_kind[2] == OMHD_BC_PERIODIC;
+  const int lm = a.lm_type;
+  const T* W = m.W;
+  for (int q = t; q < NXS + NYS; q += n) {
     int o, st;
     T *dl, *dr;
     int qq;
@@ -183,16 +203,16 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
       const int cx = q % XS, cy = q / XS;
       o = (cy + 2) * RX + (cx + 1);
       st = 1;
-      dl = SLx;
-      dr = SRx;
+      dl = m.SLx;
+      dr = m.SRx;
       qq = q;
     } else {
       qq = q - NXS;
       const int cx = qq % TX, cy = qq / TX;
       o = (cy + 1) * RX + (cx + 2);
       st = RX;
-      dl = SLy;
-      dr = SRy;
+      dl = m.SLy;
+      dr = m.SRy;
     }
     if constexpr (TAPE == tape::kNone) {
 #pragma unroll
@@ -224,50 +244,72 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
       }
     }
   }
-  __syncthreads();
-  // wall face fixes: x walls (2D_reconnection/bc.f90:136-165), y walls (2D_KH/bc.f90:55-83)
-  if (!perx || !pery) {
-    if (!perx && tid < TY * NV) {
-      const int cy = tid % TY, v = tid / TY;
-      if (gi0 == 1) {  // west face: VL = flip(VR)
-        const T s = SRx[v * NXS + cy * XS + 1];
-        SLx[v * NXS + cy * XS + 0] = ((a.bc_flip[0] >> v) & 1) ? -s : s;
-      }
-      const int cl = (ix - 2) - gi0 + 1;  // cx of the last interior cell
-      if (cl >= 1 && cl <= TX) {          // east face: VR = flip(VL)
-        const T s = SLx[v * NXS + cy * XS + cl];
-        SRx[v * NXS + cy * XS + cl + 1] = ((a.bc_flip[1] >> v) & 1) ? -s : s;
-      }
-    }
-    if (!pery && tid >= NT - TX) {
-      const int cx = tid - (NT - TX);
-      const int cl = (jx - 2) - gj0 + 1;
-      for (int v = 0; v < NV; ++v) {
-        if (gj0 == 1) {  // south face: VL = flip(VR)
-          const T s = SRy[v * NYS + 1 * TX + cx];
-          SLy[v * NYS + 0 * TX + cx] = ((a.bc_flip[2] >> v) & 1) ? -s : s;
-        }
-        if (cl >= 1 && cl <= TY) {  // north face: VR = flip(VL)
-          const T s = SLy[v * NYS + cl * TX + cx];
-          SRy[v * NYS + (cl + 1) * TX + cx] = ((a.bc_flip[3] >> v) & 1) ? -s : s;
-        }
-      }
-    }
-    __syncthreads();
-  }
+}
 
-  // ---- C: fluxes of all x faces (work items 0..NXFP-1, padded to whole
-  //      warps) and all y faces (items NXFP..NXFP+NYF-1) ----
+// wall face fixes after phase B: x walls (2D_reconnection/bc.f90:136-165),
+// y walls (2D_KH/bc.f90:55-83)
+template <class T, class G>
+__device__ __forceinline__ void phase_walls(const StageArgs& a, int bxi, int byi, const TileMem<T>& m, int t, int n) {
+  constexpr int TX = G::TX, TY = G::TY, NXS = G::NXS, NYS = G::NYS, XS = TX + 2;
+  const int ix = a.ix, jx = a.jx;
+  const int gi0 = 1 + bxi * TX, gj0 = 1 + byi * TY;
+  if (a.bc_kind[0] != OMHD_BC_PERIODIC) {
+    const int cl = (ix - 2) - gi0 + 1;  // cx of the last interior cell
+    for (int k = t; k < TY * NV; k += n) {
+      const int cy = k % TY, v = k / TY;
+      if (gi0 == 1) {  // west face: VL = flip(VR)
+        const T s = m.SRx[v * NXS + cy * XS + 1];
+        m.SLx[v * NXS + cy * XS + 0] = ((a.bc_flip[0] >> v) & 1) ? -s : s;
+      }
+      if (cl >= 1 && cl <= TX) {  // east face: VR = flip(VL)
+        const T s = m.SLx[v * NXS + cy * XS + cl];
+        m.SRx[v * NXS + cy * XS + cl + 1] = ((a.bc_flip[1] >> v) & 1) ? -s : s;
+      }
+    }
+  }
+  if (a.bc_kind[2] != OMHD_BC_PERIODIC) {
+    const int cl = (jx - 2) - gj0 + 1;
+    // the last threads of the group, so that x and y fixes run side by side
+    for (int k = n - 1 - t; k < TX * NV; k += n) {
+      const int cx = k % TX, v = k / TX;
+      if (gj0 == 1) {  // south face: VL = flip(VR)
+        const T s = m.SRy[v * NYS + 1 * TX + cx];
+        m.SLy[v * NYS + 0 * TX + cx] = ((a.bc_flip[2] >> v) & 1) ? -s : s;
+      }
+      if (cl >= 1 && cl <= TY) {  // north face: VR = flip(VL)
+        const T s = m.SLy[v * NYS + cl * TX + cx];
+        m.SRy[v * NYS + (cl + 1) * TX + cx] = ((a.bc_flip[3] >> v) & 1) ? -s : s;
+      }
+    }
+  }
+}
+
+// phase C: fluxes of all x faces (work items 0..NXFP-1, padded to whole
+// warps) and all y faces (items NXFP..NXFP+NYF-1)
+template <class T, int FLUX, class G, int TAPE>
+__device__ __forceinline__ void phase_flux(const StageArgs& a, int bxi, int byi, const TileMem<T>& m, int t, int n,
+                                           double chd) {
+  constexpr int TX = G::TX, RX = G::RX;
+  constexpr int NXS = G::NXS, NYS = G::NYS, NXF = G::NXF, NYF = G::NYF, NXFP = G::NXFP, XS = TX + 2;
+  constexpr int PL = RX * G::RY;
+  const int ix = a.ix, jx = a.jx;
+  const size_t N = (size_t)ix * jx;
+  const int gi0 = 1 + bxi * TX, gj0 = 1 + byi * G::TY;
+  const bool resist = a.eta_kind != OMHD_ETA_NONE;
+  const double gamma = a.gamma;
+  const T ch = T(chd), gam = T(gamma);
+  const T r1 = T(1.0 / (gamma - 1.0)), r2 = T(gamma / (gamma - 1.0));
+  const T* W = m.W;
   constexpr int XF = TX + 1;
-  for (int q = tid; q < NXFP + NYF; q += NT) {
+  for (int q = t; q < NXFP + NYF; q += n) {
     if (q < NXFP) {
       if (q >= NXF) continue;  // padding lanes
       const int fx = q % XF, cy = q / XF;
       T L[NV], R[NV], Fo[NV];
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        L[v] = SLx[v * NXS + cy * XS + fx];
-        R[v] = SRx[v * NXS + cy * XS + fx + 1];
+        L[v] = m.SLx[v * NXS + cy * XS + fx];
+        R[v] = m.SRx[v * NXS + cy * XS + fx + 1];
       }
       if constexpr (TAPE == tape::kNone) {
         riemann_flux<T, 1, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
@@ -295,15 +337,15 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
         }
       }
 #pragma unroll
-      for (int v = 0; v < NV; ++v) FBx[v * NXF + q] = double(Fo[v]);
+      for (int v = 0; v < NV; ++v) m.FX[v * m.fxv + cy * m.fxr + fx] = double(Fo[v]);
     } else {
       const int qq = q - NXFP;
       const int cx = qq % TX, fy = qq / TX;
       T L[NV], R[NV], Fo[NV];
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        L[v] = SLy[v * NYS + fy * TX + cx];
-        R[v] = SRy[v * NYS + (fy + 1) * TX + cx];
+        L[v] = m.SLy[v * NYS + fy * TX + cx];
+        R[v] = m.SRy[v * NYS + (fy + 1) * TX + cx];
       }
       if constexpr (TAPE == tape::kNone) {
         riemann_flux<T, 2, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
@@ -331,74 +373,107 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
         }
       }
 #pragma unroll
-      for (int v = 0; v < NV; ++v) FBy[v * NYF + qq] = double(Fo[v]);
+      for (int v = 0; v < NV; ++v) m.FY[v * m.fyv + fy * TX + cx] = double(Fo[v]);
     }
   }
-  __syncthreads();
+}
 
-  // ---- D: update, ghost fill, GLM, CFL ----
+// phase D: update, ghost fill, GLM, CFL of the tile's cells t, t+n, ...;
+// returns this thread's largest CFL speed (stage 2) or 0
+template <class T, class G>
+__device__ __forceinline__ double phase_update(const StageArgs& a, int bxi, int byi, const TileMem<T>& m, int t,
+                                               int n, double dt, double glmf) {
+  constexpr int TX = G::TX, TY = G::TY;
+  const int ix = a.ix, jx = a.jx;
+  const size_t N = (size_t)ix * jx;
+  const int gi0 = 1 + bxi * TX, gj0 = 1 + byi * TY;
+  const bool perx = a.bc_kind[0] == OMHD_BC_PERIODIC, pery = a.bc_kind[2] == OMHD_BC_PERIODIC;
+  const double gamma = a.gamma;
+  const double f1g = gamma - 1;
   double vcell = 0.0;
-  if (tid < TX * TY) {
-    const int tx = tid % TX, ty = tid / TX;
+  for (int k = t; k < TX * TY; k += n) {
+    const int tx = k % TX, ty = k / TX;
     const int gi = gi0 + tx, gj = gj0 + ty;
-    if (gi <= ix - 2 && gj <= jx - 2) {
-      const double dtx = a.dtx_scale * dt / a.dx, dty = a.dtx_scale * dt / a.dy;
-      const size_t c = (size_t)gi + (size_t)ix * gj;
-      double out[NV];
+    if (gi > ix - 2 || gj > jx - 2) continue;
+    const double dtx = a.dtx_scale * dt / a.dx, dty = a.dtx_scale * dt / a.dy;
+    const size_t c = (size_t)gi + (size_t)ix * gj;
+    double out[NV];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        // F(i-1/2) - F(i+1/2) in FP64
-        const double dF = FBx[v * NXF + ty * XF + tx] - FBx[v * NXF + ty * XF + tx + 1];
-        const double gm = FBy[v * NYF + ty * TX + tx], gp = FBy[v * NYF + (ty + 1) * TX + tx];
-        double d;
-        if (a.iso)
-          d = dtx * (dF + gm - gp);  // rk.f90:26-35 operation order
-        else
-          d = dtx * dF + dty * (gm - gp);
-        double ub = a.Ubase[v * N + c];
-        if (v == PS) ub = glmf * ub;
-        if (a.stage == 1 || a.time_type == OMHD_TIME_RK2)
-          out[v] = ub + d;  // rk_tvd21 / rk_std21 / rk_std22
-        else
-          out[v] = 0.5 * (ub + a.U1[v * N + c] + d);  // rk_tvd22 (rk.f90:56-66)
-      }
-      if (a.stage == 2) out[PS] = glmf * out[PS];  // second GLM half (main.f90:185)
+    for (int v = 0; v < NV; ++v) {
+      // F(i-1/2) - F(i+1/2) in FP64
+      const double* fx = m.FX + v * m.fxv + ty * m.fxr + tx;
+      const double dF = fx[0] - fx[1];
+      const double gm = m.FY[v * m.fyv + ty * TX + tx], gp = m.FY[v * m.fyv + (ty + 1) * TX + tx];
+      double d;
+      if (a.iso)
+        d = dtx * (dF + gm - gp);  // rk.f90:26-35 operation order
+      else
+        d = dtx * dF + dty * (gm - gp);
+      double ub = a.Ubase[v * N + c];
+      if (v == PS) ub = glmf * ub;
+      if (a.stage == 1 || a.time_type == OMHD_TIME_RK2)
+        out[v] = ub + d;  // rk_tvd21 / rk_std21 / rk_std22
+      else
+        out[v] = 0.5 * (ub + a.U1[v * N + c] + d);  // rk_tvd22 (rk.f90:56-66)
+    }
+    if (a.stage == 2) out[PS] = glmf * out[PS];  // second GLM half (main.f90:185)
 
-      // owner-writes ghost fill (bc.f90 order: x sides, then y sides)
-      int xt[3], yt[3], xf[3], yf[3], nxt = 1, nyt = 1;
-      xt[0] = gi;
-      xf[0] = 0;
-      yt[0] = gj;
-      yf[0] = 0;
-      if (gi == 1) { xt[nxt] = perx ? ix - 1 : 0; xf[nxt] = perx ? 0 : a.bc_flip[0]; ++nxt; }
-      if (gi == ix - 2) { xt[nxt] = perx ? 0 : ix - 1; xf[nxt] = perx ? 0 : a.bc_flip[1]; ++nxt; }
-      if (gj == 1) { yt[nyt] = pery ? jx - 1 : 0; yf[nyt] = pery ? 0 : a.bc_flip[2]; ++nyt; }
-      if (gj == jx - 2) { yt[nyt] = pery ? 0 : jx - 1; yf[nyt] = pery ? 0 : a.bc_flip[3]; ++nyt; }
-      for (int b = 0; b < nyt; ++b)
-        for (int q = 0; q < nxt; ++q) {
-          const size_t cc = (size_t)xt[q] + (size_t)ix * yt[b];
-          const int fm = xf[q] ^ yf[b];
+    // owner-writes ghost fill (bc.f90 order: x sides, then y sides)
+    int xt[3], yt[3], xf[3], yf[3], nxt = 1, nyt = 1;
+    xt[0] = gi;
+    xf[0] = 0;
+    yt[0] = gj;
+    yf[0] = 0;
+    if (gi == 1) { xt[nxt] = perx ? ix - 1 : 0; xf[nxt] = perx ? 0 : a.bc_flip[0]; ++nxt; }
+    if (gi == ix - 2) { xt[nxt] = perx ? 0 : ix - 1; xf[nxt] = perx ? 0 : a.bc_flip[1]; ++nxt; }
+    if (gj == 1) { yt[nyt] = pery ? jx - 1 : 0; yf[nyt] = pery ? 0 : a.bc_flip[2]; ++nyt; }
+    if (gj == jx - 2) { yt[nyt] = pery ? 0 : jx - 1; yf[nyt] = pery ? 0 : a.bc_flip[3]; ++nyt; }
+    for (int b = 0; b < nyt; ++b)
+      for (int q = 0; q < nxt; ++q) {
+        const size_t cc = (size_t)xt[q] + (size_t)ix * yt[b];
+        const int fm = xf[q] ^ yf[b];
 #pragma unroll
-          for (int v = 0; v < NV; ++v) a.Uout[v * N + cc] = ((fm >> v) & 1) ? -out[v] : out[v];
-        }
-
-      if (a.stage == 2) {  // set_dt.f90:27-37 on the new state
-        const double ro = out[RO];
-        const double iro = rcp_<double, OMHD_FAST>(ro);  // one reciprocal for the three velocities
-        const double vx = divr_<double, OMHD_FAST>(out[MX], ro, iro), vy = divr_<double, OMHD_FAST>(out[MY], ro, iro),
-                     vz = divr_<double, OMHD_FAST>(out[MZ], ro, iro);
-        const double rv2 = vx * out[MX] + vy * out[MY] + vz * out[MZ];
-        const double B2 = out[BX] * out[BX] + out[BY] * out[BY] + out[BZ] * out[BZ];
-        const double pr = f1g * (out[EN] - 0.5 * (rv2 + B2));
-        const double f1 = gamma * pr;
-        const double vfx = fast_speed<double, OMHD_FAST>(f1, B2, out[BX], ro);
-        const double vfy = fast_speed<double, OMHD_FAST>(f1, B2, out[BY], ro);
-        const double sx = fabs(vx) + vfx, sy = fabs(vy) + vfy;
-        vcell = lt_<double, OMHD_FAST>(sx, sy) ? sy : sx;  // fmax2(sx, sy)
+        for (int v = 0; v < NV; ++v) a.Uout[v * N + cc] = ((fm >> v) & 1) ? -out[v] : out[v];
       }
+
+    if (a.stage == 2) {  // set_dt.f90:27-37 on the new state
+      const double ro = out[RO];
+      const double iro = rcp_<double, OMHD_FAST>(ro);  // one reciprocal for the three velocities
+      const double vx = divr_<double, OMHD_FAST>(out[MX], ro, iro), vy = divr_<double, OMHD_FAST>(out[MY], ro, iro),
+                   vz = divr_<double, OMHD_FAST>(out[MZ], ro, iro);
+      const double rv2 = vx * out[MX] + vy * out[MY] + vz * out[MZ];
+      const double B2 = out[BX] * out[BX] + out[BY] * out[BY] + out[BZ] * out[BZ];
+      const double pr = f1g * (out[EN] - 0.5 * (rv2 + B2));
+      const double f1 = gamma * pr;
+      const double vfx = fast_speed<double, OMHD_FAST>(f1, B2, out[BX], ro);
+      const double vfy = fast_speed<double, OMHD_FAST>(f1, B2, out[BY], ro);
+      const double sx = fabs(vx) + vfx, sy = fabs(vy) + vfy;
+      const double sc = lt_<double, OMHD_FAST>(sx, sy) ? sy : sx;  // fmax2(sx, sy)
+      vcell = lt_<double, OMHD_FAST>(vcell, sc) ? sc : vcell;
     }
   }
   return vcell;
+}
+
+// One stage on one tile (tile coordinates bxi, byi) of the grid described by
+// `a`, by all threads of the CTA; returns this thread's CFL speed of the
+// updated cells (stage 2) or 0.  Three or four CTA-wide barriers.
+template <class T, int FLUX, class G, int TAPE = tape::kNone>
+__device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int byi, unsigned char* smem_raw,
+                                               double dt, double chd, double glmf) {
+  const TileMem<T> m = tile_mem_separate<T, G>(smem_raw);
+  const int tid = threadIdx.x;
+  phase_load<T, G>(a, bxi, byi, m, tid, G::NT, glmf);
+  __syncthreads();
+  phase_recon<T, G, TAPE>(a, bxi, byi, m, tid, G::NT);
+  __syncthreads();
+  if (a.bc_kind[0] != OMHD_BC_PERIODIC || a.bc_kind[2] != OMHD_BC_PERIODIC) {
+    phase_walls<T, G>(a, bxi, byi, m, tid, G::NT);
+    __syncthreads();
+  }
+  phase_flux<T, FLUX, G, TAPE>(a, bxi, byi, m, tid, G::NT, chd);
+  __syncthreads();
+  return phase_update<T, G>(a, bxi, byi, m, tid, G::NT, dt, glmf);
 }
 
 // one CTA per tile of one grid
@@ -421,6 +496,129 @@ __global__ void __launch_bounds__(GeoFor<T>::type::NT) k_stage2d(const StageArgs
     StepConsts sc{a.cfl, a.dmin, a.dx, a.eta_kind};
     reduce_and_finalize(st, sc, a.err, bm, gridDim.x * gridDim.y, 1);
   }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 pipelined stage kernel: one persistent CTA per SM, warp-specialised.
+// The flux phase C is FP64-pipe bound (~96 % of the pipe), while the load +
+// u2v phase A, the slope phase B and the update phase D are latency bound
+// (~50 %).  So NPW producer warps run A and B (+ wall fixes) of tile i+1
+// while the 9 consumer warps run C and D of tile i: two face-state buffers in
+// shared memory, handed over with named barriers (FULL[b]: producers arrive,
+// consumers wait; EMPTY[b]: consumers arrive after D, producers wait before
+// refilling b).  Fluxes overwrite the lower-cell face state that only their
+// own face reads, so a buffer is 4 face-state arrays (83 KB) and the CTA holds
+// W + 2 buffers = 195 KB.  Non-resistive 2D runs (the resistive terms read W
+// in phase C, which the producers already refill).
+// ---------------------------------------------------------------------------
+using PipeGeo = Geo2<16, 16>;
+constexpr int kPipeBarProd = 1, kPipeBarCons = 2, kPipeBarFull = 3, kPipeBarEmpty = 5;
+
+__device__ __forceinline__ void named_bar_sync(int id, int n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+__device__ __forceinline__ void named_bar_arrive(int id, int n) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+constexpr size_t pipe_smem_bytes() {
+  return sizeof(double) * (size_t)NV * (PipeGeo::RX * PipeGeo::RY + 2 * 2 * (PipeGeo::NXS + PipeGeo::NYS));
+}
+
+__device__ __forceinline__ TileMem<double> pipe_mem(unsigned char* smem_raw, int b) {
+  using G = PipeGeo;
+  TileMem<double> m;
+  m.W = reinterpret_cast<double*>(smem_raw);
+  m.SLx = m.W + NV * G::RX * G::RY + (size_t)b * NV * 2 * (G::NXS + G::NYS);
+  m.SRx = m.SLx + NV * G::NXS;
+  m.SLy = m.SRx + NV * G::NXS;
+  m.SRy = m.SLy + NV * G::NYS;
+  m.FX = m.SLx;  // flux of x face (fx, cy) in the SLx slot of cell fx of row cy
+  m.fxv = G::NXS;
+  m.fxr = G::TX + 2;
+  m.FY = m.SLy;  // flux of y face (cx, fy) in the SLy slot of cell fy of column cx
+  m.fyv = G::NYS;
+  return m;
+}
+
+template <int FLUX, int TAPE, int NPW>
+__global__ void __launch_bounds__(NPW * 32 + PipeGeo::NT, 1) k_stage2d_pipe(const StageArgs a) {
+  using G = PipeGeo;
+  constexpr int NP = NPW * 32, NC = G::NT, NTOT = NP + NC;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red32[32];
+  __shared__ int skip;
+  StepState* st = a.st;
+  if (threadIdx.x == 0) skip = st->done || *(volatile int*)&a.err->code;
+  __syncthreads();
+  if (skip) return;
+  const double dt = st->dt, chd = st->ch, glmf = st->glm_f;
+  const int ntx = (a.ix - 2 + G::TX - 1) / G::TX;
+  const int ntiles = ntx * ((a.jx - 2 + G::TY - 1) / G::TY);
+  const bool walls = a.bc_kind[0] != OMHD_BC_PERIODIC || a.bc_kind[2] != OMHD_BC_PERIODIC;
+  double vmax = 0.0;
+  if (threadIdx.x < NP) {  // producers: A, B, wall fixes of tiles blockIdx.x, +gridDim.x, ...
+    const int t = threadIdx.x;
+    int i = 0;
+    for (int w = blockIdx.x; w < ntiles; w += gridDim.x, ++i) {
+      const int b = i & 1;
+      const TileMem<double> m = pipe_mem(smem_raw, b);
+      if (i >= 2) named_bar_sync(kPipeBarEmpty + b, NTOT);  // consumers are done with buffer b
+      if (i >= 1) named_bar_sync(kPipeBarProd, NP);         // W of the previous tile is read
+      phase_load<double, G>(a, w % ntx, w / ntx, m, t, NP, glmf);
+      named_bar_sync(kPipeBarProd, NP);
+      phase_recon<double, G, TAPE>(a, w % ntx, w / ntx, m, t, NP);
+      if (walls) {
+        named_bar_sync(kPipeBarProd, NP);
+        phase_walls<double, G>(a, w % ntx, w / ntx, m, t, NP);
+      }
+      __threadfence_block();
+      named_bar_arrive(kPipeBarFull + b, NTOT);
+    }
+  } else {  // consumers: C, D of the same tiles, one tile behind
+    const int t = threadIdx.x - NP;
+    const int nmine = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    int i = 0;
+    for (int w = blockIdx.x; w < ntiles; w += gridDim.x, ++i) {
+      const int b = i & 1;
+      const TileMem<double> m = pipe_mem(smem_raw, b);
+      named_bar_sync(kPipeBarFull + b, NTOT);
+      phase_flux<double, FLUX, G, TAPE>(a, w % ntx, w / ntx, m, t, NC, chd);
+      named_bar_sync(kPipeBarCons, NC);
+      const double v = phase_update<double, G>(a, w % ntx, w / ntx, m, t, NC, dt, glmf);
+      vmax = lt_<double, OMHD_FAST>(vmax, v) ? v : vmax;
+      if (i + 2 < nmine) {  // the producers refill buffer b for tile i+2
+        __threadfence_block();
+        named_bar_arrive(kPipeBarEmpty + b, NTOT);
+      }
+    }
+  }
+  if (a.stage == 2) {
+    const double bm = block_max_pos(vmax, red32);
+    StepConsts sc{a.cfl, a.dmin, a.dx, a.eta_kind};
+    reduce_and_finalize(st, sc, a.err, bm, gridDim.x, 1);
+  }
+}
+
+template <int FLUX, int TAPE, int NPW = 3>
+int launch_pipe(const StageArgs& a, cudaStream_t s) {
+  const size_t bytes = pipe_smem_bytes();
+  static bool configured = false;
+  static int nsm = 0;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_stage2d_pipe<FLUX, TAPE, NPW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)bytes);
+    if (e != cudaSuccess) return (int)e;
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return (int)e;
+    configured = true;
+  }
+  const int ntiles = ((a.ix - 2 + PipeGeo::TX - 1) / PipeGeo::TX) * ((a.jx - 2 + PipeGeo::TY - 1) / PipeGeo::TY);
+  const int grid = ntiles < nsm ? ntiles : nsm;
+  k_stage2d_pipe<FLUX, TAPE, NPW><<<grid, NPW * 32 + PipeGeo::NT, bytes, s>>>(a);
+  return (int)cudaGetLastError();
 }
 
 // Ensemble of independent 2D grids in one persistent launch: CTAs loop over

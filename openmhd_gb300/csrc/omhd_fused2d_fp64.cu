@@ -13,6 +13,7 @@ int launch_stage2d_fp64(const StageArgs& a, cudaStream_t s) {
     StageArgs b = a;
     b.tlim = nullptr;
     b.tface = nullptr;
+    if (a.eta_kind == OMHD_ETA_NONE) return v_fp64::launch_pipe<FX_HLLD, tape::kRecord>(b, s);
     return v_fp64::launch_one<double, FX_HLLD, tape::kRecord>(b, s);
   }
   return v_fp64::launch_variant<double>(a, s);
@@ -20,7 +21,10 @@ int launch_stage2d_fp64(const StageArgs& a, cudaStream_t s) {
 int launch_stage2d_fp64_tape(const StageArgs& a, int mode, cudaStream_t s) {
   if (a.flux_type != FX_HLLD || a.nd != 2 || !a.tlim || !a.tface) return (int)cudaErrorInvalidValue;
   if (a.lm_type != LM_MINMOD && a.lm_type != LM_MC) return (int)cudaErrorInvalidValue;
-  if (mode == tape::kRecord) return v_fp64::launch_one<double, FX_HLLD, tape::kRecord>(a, s);
+  if (mode == tape::kRecord) {
+    if (a.eta_kind == OMHD_ETA_NONE) return v_fp64::launch_pipe<FX_HLLD, tape::kRecord>(a, s);
+    return v_fp64::launch_one<double, FX_HLLD, tape::kRecord>(a, s);
+  }
   if (mode == tape::kReplay) return v_fp64::launch_one<double, FX_HLLD, tape::kReplay>(a, s);
   return (int)cudaErrorInvalidValue;
 }

@@ -217,6 +217,28 @@ __device__ __forceinline__ void reconstruct_t(int type, T wm, T w0, T wp, T& lef
     reconstruct<T>(type, wm, w0, wp, left, right);
 }
 
+// HLLD intermediate (star) state of one side (flux_solver.f90:482-493 for L,
+// :496-507 for R, the same expressions with the side's values): side state
+// rho, normal / tangential velocities, tangential fields, wave speed a, total
+// energy E, total pressure pts, v.B, star density ros = rho*(a - un)/(a - aM)
+// and ie = 1/(a - aM); returns the star state's conserved variables in S and
+// its tangential velocities in v1, v2.
+template <class T, bool FAST, int vn, int vt1, int vt2, int bt1, int bt2, int mn, int mt1, int mt2>
+__device__ __forceinline__ void star_state(T ro, T un, T ut1, T ut2, T b1, T b2, T a, T E, T pts, T vB, T ros, T ie,
+                                           T aM, T pt, T Bn, T (&S)[NV], T& v1, T& v2) {
+  const T t = a - un;
+  const T f = rcp_<T, FAST>(ro * t * (a - aM) - Bn * Bn);
+  S[bt1] = b1 * f * (ro * (t * t) - Bn * Bn);
+  S[bt2] = b2 * f * (ro * (t * t) - Bn * Bn);
+  v1 = ut1 - f * Bn * b1 * (aM - un);
+  v2 = ut2 - f * Bn * b2 * (aM - un);
+  S[RO] = ros;
+  S[EN] = divr_<T, FAST>((t * E - pts * un + pt * aM + Bn * (vB - aM * Bn - v1 * S[bt1] - v2 * S[bt2])), (a - aM), ie);
+  S[mn] = ros * aM;
+  S[mt1] = ros * v1;
+  S[mt2] = ros * v2;
+}
+
 // Numerical flux across one face (2D_basic/flux_solver.f90):
 //   LLF :89-148, HLL :153-221, HLLC :226-347, HLLD :352-585 (HLLC-G fallback
 //   :447-476), LHLLD :590-789; GLM fluxes for Bn and psi :580-581.
@@ -460,6 +482,66 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
         Fo[mt2] = f1 * (aL * (roL * at2 - UL[mt2]) + FL[mt2]) + f2 * (aR * (roR * at2 - UR[mt2]) + FR[mt2]);
         Fo[EN] = f1 * (aL * (enL - UL[EN]) + FL[EN]) + f2 * (aR * (enR - UR[EN]) + FR[EN]);
         Fo[RO] = f1 * (aL * (roL - L[RO]) + FL[RO]) + f2 * (aR * (roR - R[RO]) + FR[RO]);
+      } else if constexpr (kF64) {
+        // Side-selected intermediate states (FAST FP64).  The region picks the
+        // side s whose state the flux uses (F(L*) and F(L**): L; F(R*) and
+        // F(R**): R); every lane builds the star state of its own side from
+        // selected inputs, so a warp whose faces take different sides runs one
+        // star-state computation, not both; the central states (both sides)
+        // add the other side's star state.  The L* and R* formulas of
+        // :482-507 are mirror images, so the selected inputs give them exactly;
+        // the central states :533-572 are written symmetrically in (s, o)
+        // with sigma = +1 for s = L and -1 for s = R: (UR1 - UL1) = sigma (O1 - S1).
+        aL1 = aM - aVL;
+        aR1 = aM + aVR;
+        const bool sLs = decide<TAPE>(ge0_<T, FAST>(aL1), code, tape::kLS);
+        const bool sRs = !sLs && decide<TAPE>(le0_<T, FAST>(aR1), code, tape::kRS);
+        const bool cen = !sLs && !sRs;
+        const bool sR = sRs || (cen && !decide<TAPE>(ge0_<T, FAST>(aM), code, tape::kSSLeft));
+        const T Bn = Uh[bn];
+        T S1[NV] = {}, vs1, vs2;
+        star_state<T, FAST, vn, vt1, vt2, bt1, bt2, mn, mt1, mt2>(
+            sR ? R[RO] : L[RO], sR ? R[vn] : L[vn], sR ? R[vt1] : L[vt1], sR ? R[vt2] : L[vt2],
+            sR ? R[bt1] : L[bt1], sR ? R[bt2] : L[bt2], sR ? aR : aL, sR ? UR[EN] : UL[EN], sR ? ptR : ptL,
+            sR ? vBR : vBL, sR ? roR : roL, sR ? ieR : ieL, aM, pt, Bn, S1, vs1, vs2);
+        const T as = sR ? aR : aL;
+        T gs[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) gs[v] = sR ? gR[v] : gL[v];
+        if (!cen) {  // F(L*) :514-519 / F(R*) :522-527: a*(U* - U) + F = a*U* - g
+#pragma unroll
+          for (int v = MX; v <= EN; ++v) Fo[v] = as * S1[v] - gs[v];
+          Fo[RO] = as * S1[RO] - gs[RO];
+          Fo[bt1] = as * S1[bt1] - gs[bt1];
+          Fo[bt2] = as * S1[bt2] - gs[bt2];
+        } else {  // central states :533-572
+          T O1[NV] = {}, vo1, vo2;
+          star_state<T, FAST, vn, vt1, vt2, bt1, bt2, mn, mt1, mt2>(
+              sR ? L[RO] : R[RO], sR ? L[vn] : R[vn], sR ? L[vt1] : R[vt1], sR ? L[vt2] : R[vt2],
+              sR ? L[bt1] : R[bt1], sR ? L[bt2] : R[bt2], sR ? aL : aR, sR ? UL[EN] : UR[EN], sR ? ptL : ptR,
+              sR ? vBL : vBR, sR ? roL : roR, sR ? ieL : ieR, aM, pt, Bn, O1, vo1, vo2);
+          const T ros = sR ? roR : roL, roo = sR ? roL : roR;
+          const T rss = ros * (sR ? rsR : rsL), rso = roo * (sR ? rsL : rsR);  // sqrt(rho*) of s and o
+          f1 = rcp_<T, FAST>(rss + rso);
+          const T f2 = (TAPE == tape::kNone) ? fsign(T(1), Bn) : (bneg ? T(-1) : T(1));
+          const T f2s = sR ? -f2 : f2;
+          T U2[NV];
+          const T at1 = f1 * (rss * vs1 + rso * vo1 + (O1[bt1] - S1[bt1]) * f2s);
+          const T at2 = f1 * (rss * vs2 + rso * vo2 + (O1[bt2] - S1[bt2]) * f2s);
+          U2[bt1] = f1 * (rss * O1[bt1] + rso * S1[bt1] + rss * rso * (vo1 - vs1) * f2s);
+          U2[bt2] = f1 * (rss * O1[bt2] + rso * S1[bt2] + rss * rso * (vo2 - vs2) * f2s);
+          U2[RO] = ros;
+          U2[EN] = S1[EN] - rss * (vs1 * S1[bt1] + vs2 * S1[bt2] - at1 * U2[bt1] - at2 * U2[bt2]) * f2s;
+          U2[mn] = ros * aM;
+          U2[mt1] = ros * at1;
+          U2[mt2] = ros * at2;
+          const T as1 = sR ? aR1 : aL1;
+#pragma unroll
+          for (int v = MX; v <= EN; ++v) Fo[v] = as1 * U2[v] - (as1 - as) * S1[v] - gs[v];
+          Fo[RO] = as1 * U2[RO] - (as1 - as) * S1[RO] - gs[RO];
+          Fo[bt1] = as1 * U2[bt1] - (as1 - as) * S1[bt1] - gs[bt1];
+          Fo[bt2] = as1 * U2[bt2] - (as1 - as) * S1[bt2] - gs[bt2];
+        }
       } else {
         // Region first (aL1, aR1 need only aM and the Alfven speeds), then the
         // intermediate states that region uses: F(L*) needs L* only, F(R*)
