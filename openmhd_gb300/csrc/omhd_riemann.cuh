@@ -228,10 +228,12 @@ __device__ __forceinline__ void star_state(T ro, T un, T ut1, T ut2, T b1, T b2,
                                            T aM, T pt, T Bn, T (&S)[NV], T& v1, T& v2) {
   const T t = a - un;
   const T f = rcp_<T, FAST>(ro * t * (a - aM) - Bn * Bn);
-  S[bt1] = b1 * f * (ro * (t * t) - Bn * Bn);
-  S[bt2] = b2 * f * (ro * (t * t) - Bn * Bn);
-  v1 = ut1 - f * Bn * b1 * (aM - un);
-  v2 = ut2 - f * Bn * b2 * (aM - un);
+  const T fb = f * (ro * (t * t) - Bn * Bn);  // B_t* = B_t fb, v_t* = v_t - B_t fv
+  const T fv = f * Bn * (aM - un);
+  S[bt1] = b1 * fb;
+  S[bt2] = b2 * fb;
+  v1 = ut1 - fv * b1;
+  v2 = ut2 - fv * b2;
   S[RO] = ros;
   S[EN] = divr_<T, FAST>((t * E - pts * un + pt * aM + Bn * (vB - aM * Bn - v1 * S[bt1] - v2 * S[bt2])), (a - aM), ie);
   S[mn] = ros * aM;
@@ -285,10 +287,16 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   UL[MZ] = L[RO] * L[VZ];
   UL[EN] = T(0.5) * (L[RO] * v2 + B2) + r1 * L[PR];
   FL[RO] = L[RO] * L[vn];
-  FL[mn] = L[RO] * L[vn] * L[vn] - L[bn] * L[bn] + L[PR] + T(0.5) * B2;
+  if constexpr (kF64) {  // with pt = p + B^2/2: rho vn^2 + pt - bn^2 and (E + pt) vn - (v.B) bn (r2 = r1 + 1)
+    const T pt_ = L[PR] + T(0.5) * B2;
+    FL[mn] = UL[mn] * L[vn] + pt_ - L[bn] * L[bn];
+    FL[EN] = (UL[EN] + pt_) * L[vn] - vBL * L[bn];
+  } else {
+    FL[mn] = L[RO] * L[vn] * L[vn] - L[bn] * L[bn] + L[PR] + T(0.5) * B2;
+    FL[EN] = (T(0.5) * L[RO] * v2 + r2 * L[PR] + B2) * L[vn] - vBL * L[bn];
+  }
   FL[mt1] = L[RO] * L[vn] * L[vt1] - L[bn] * L[bt1];
   FL[mt2] = L[RO] * L[vn] * L[vt2] - L[bn] * L[bt2];
-  FL[EN] = (T(0.5) * L[RO] * v2 + r2 * L[PR] + B2) * L[vn] - vBL * L[bn];
   FL[bt1] = L[vn] * L[bt1] - L[bn] * L[vt1];
   FL[bt2] = L[vn] * L[bt2] - L[bn] * L[vt2];
   f1 = gamma * L[PR];
@@ -318,10 +326,16 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   UR[MZ] = R[RO] * R[VZ];
   UR[EN] = T(0.5) * (R[RO] * v2 + B2) + r1 * R[PR];
   FR[RO] = R[RO] * R[vn];
-  FR[mn] = R[RO] * R[vn] * R[vn] - R[bn] * R[bn] + R[PR] + T(0.5) * B2;
+  if constexpr (kF64) {  // with pt = p + B^2/2: rho vn^2 + pt - bn^2 and (E + pt) vn - (v.B) bn (r2 = r1 + 1)
+    const T pt_ = R[PR] + T(0.5) * B2;
+    FR[mn] = UR[mn] * R[vn] + pt_ - R[bn] * R[bn];
+    FR[EN] = (UR[EN] + pt_) * R[vn] - vBR * R[bn];
+  } else {
+    FR[mn] = R[RO] * R[vn] * R[vn] - R[bn] * R[bn] + R[PR] + T(0.5) * B2;
+    FR[EN] = (T(0.5) * R[RO] * v2 + r2 * R[PR] + B2) * R[vn] - vBR * R[bn];
+  }
   FR[mt1] = R[RO] * R[vn] * R[vt1] - R[bn] * R[bt1];
   FR[mt2] = R[RO] * R[vn] * R[vt2] - R[bn] * R[bt2];
-  FR[EN] = (T(0.5) * R[RO] * v2 + r2 * R[PR] + B2) * R[vn] - vBR * R[bn];
   FR[bt1] = R[vn] * R[bt1] - R[bn] * R[vt1];
   FR[bt2] = R[vn] * R[bt2] - R[bn] * R[vt2];
   f1 = gamma * R[PR];
@@ -665,8 +679,14 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
     }
   }
   // GLM fluxes :580-581
-  Fo[bn] = T(0.5) * ((L[PS] + R[PS]) - ch * (R[bn] - L[bn]));
-  Fo[PS] = T(0.5) * (ch2 * (L[bn] + R[bn]) - ch * (R[PS] - L[PS]));
+  if constexpr (kF64) {  // the halving folded into the (exact) half speeds
+    const T hch = T(0.5) * ch, hch2 = T(0.5) * ch2;
+    Fo[bn] = T(0.5) * (L[PS] + R[PS]) - hch * (R[bn] - L[bn]);
+    Fo[PS] = hch2 * (L[bn] + R[bn]) - hch * (R[PS] - L[PS]);
+  } else {
+    Fo[bn] = T(0.5) * ((L[PS] + R[PS]) - ch * (R[bn] - L[bn]));
+    Fo[PS] = T(0.5) * (ch2 * (L[bn] + R[bn]) - ch * (R[PS] - L[PS]));
+  }
   if constexpr (TAPE == tape::kRecord) *code_io = code_reg;
 }
 
