@@ -284,11 +284,118 @@ __device__ __forceinline__ void phase_walls(const StageArgs& a, int bxi, int byi
   }
 }
 
+// y faces in x orientation: slot k of the rotated state holds component
+// rot(k) (vx <- vy, vy <- vz, vz <- vx and the same for B, the order
+// flux_solver.f90:62-70 uses for the y direction), and the x-oriented flux
+// slot k belongs to component rot(k)
+__device__ __forceinline__ constexpr int rot_y(int k) {
+  return (k <= 2) ? (k + 1) % 3 : ((k >= 5 && k <= 7) ? 5 + (k - 4) % 3 : k);
+}
+
+// phase C for the FAST FP64 variant: the x faces (items 0..NXF-1) and the y
+// faces (items NXF..NXF+NYF-1) through one x-oriented Riemann solver, the y
+// faces' components rotated on load and back on store, so that the 544 faces
+// of a 16x16 tile fill 17 whole warps (the per-direction form below pads each
+// direction to whole warps: 18).
+template <class T, int FLUX, class G, int TAPE>
+__device__ __forceinline__ void phase_flux_rot(const StageArgs& a, int bxi, int byi, const TileMem<T>& m, int t,
+                                               int n, double chd) {
+  constexpr int TX = G::TX, RX = G::RX;
+  constexpr int NXS = G::NXS, NYS = G::NYS, NXF = G::NXF, NYF = G::NYF, XS = TX + 2, XF = TX + 1;
+  constexpr int PL = RX * G::RY;
+  const int ix = a.ix, jx = a.jx;
+  const size_t N = (size_t)ix * jx;
+  const int gi0 = 1 + bxi * TX, gj0 = 1 + byi * G::TY;
+  const bool resist = a.eta_kind != OMHD_ETA_NONE;
+  const double gamma = a.gamma;
+  const T ch = T(chd), gam = T(gamma);
+  const T r1 = T(1.0 / (gamma - 1.0)), r2 = T(gamma / (gamma - 1.0));
+  const T* W = m.W;
+  for (int q = t; q < NXF + NYF; q += n) {
+    const bool xd = q < NXF;
+    const int qq = xd ? q : q - NXF;
+    // x face (fx, cy): lower cell fx of x row cy; y face (cx, fy): lower cell
+    // fy of y column cx
+    const int fa = xd ? qq % XF : qq % TX, fb = xd ? qq / XF : qq / TX;
+    const T* bl = xd ? m.SLx + fb * XS + fa : m.SLy + fb * TX + fa;
+    const T* br = xd ? m.SRx + fb * XS + fa + 1 : m.SRy + (fb + 1) * TX + fa;
+    const int sv = xd ? NXS : NYS;
+    T L[NV], R[NV], Fo[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const int pv = (xd ? k : rot_y(k)) * sv;
+      L[k] = bl[pv];
+      R[k] = br[pv];
+    }
+    if constexpr (TAPE == tape::kNone) {
+      riemann_flux<T, 1, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
+    } else {
+      size_t tc;
+      if (xd) {  // face between cells gi0-1+fx and gi0+fx of row gj0+cy
+        const int gl = gi0 - 1 + fa, gj = gj0 + fb;
+        tc = (size_t)(gl < 0 ? 0 : (gl > ix - 2 ? ix - 2 : gl)) + (size_t)ix * (gj > jx - 2 ? jx - 2 : gj);
+      } else {  // face between rows gj0-1+fy and gj0+fy of column gi0+cx
+        const int gl = gj0 - 1 + fb, gi = gi0 + fa;
+        tc = N + (size_t)(gi > ix - 2 ? ix - 2 : gi) + (size_t)ix * (gl < 0 ? 0 : (gl > jx - 2 ? jx - 2 : gl));
+      }
+      unsigned k = (TAPE == tape::kReplay) ? a.tface[tc] : 0u;
+      riemann_flux<T, 1, FLUX, OMHD_FAST, TAPE>(L, R, ch, gam, r1, r2, Fo, &k);
+      if (TAPE == tape::kRecord && a.tface) {
+        const bool own = xd ? ((fa >= 1 || gi0 == 1) && gi0 - 1 + fa <= ix - 2 && gj0 + fb <= jx - 2)
+                            : ((fb >= 1 || gj0 == 1) && gj0 - 1 + fb <= jx - 2 && gi0 + fa <= ix - 2);
+        if (own) a.tface[tc] = (unsigned short)k;
+      }
+    }
+    double F[NV];  // back to the grid's component order
+#pragma unroll
+    for (int k = 0; k < NV; ++k) F[rot_y(k)] = xd ? double(Fo[rot_y(k)]) : double(Fo[k]);
+    if (resist) {
+      if (xd) {  // 2D_reconnection/flux_resistive.f90:266-283
+        const int fx = fa, cy = fb, g = gi0 - 1 + fx, gj = gj0 + cy;
+        if (g >= 0 && g <= ix - 2 && gj <= jx - 2) {
+          const int o = (cy + 2) * RX + (fx + 1);  // region index of cell g
+          auto B = [&](int var, int dxo, int dyo) { return double(W[var * PL + o + dxo + dyo * RX]); };
+          const double odx = 1.0 / a.dx;
+          const double eta_dx = eta_at(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gj], 0.0) * odx;
+          const double JyS = -eta_dx * (B(BZ, 1, 0) - B(BZ, 0, 0));
+          const double JzS = eta_dx * ((B(BY, 1, 0) - B(BY, 0, 0)) -
+                                       0.25 * (B(BX, 0, 1) + B(BX, 1, 1) - B(BX, 0, -1) - B(BX, 1, -1)));
+          F[EN] = F[EN] + 0.5 * (JyS * (B(BZ, 0, 0) + B(BZ, 1, 0)) - JzS * (B(BY, 0, 0) + B(BY, 1, 0)));
+          F[BY] = F[BY] - JzS;
+          F[BZ] = F[BZ] + JyS;
+        }
+      } else {  // 2D_reconnection/flux_resistive.f90:289-306
+        const int cx = fa, fy = fb, gi = gi0 + cx, g = gj0 - 1 + fy;
+        if (g >= 0 && g <= jx - 2 && gi <= ix - 2) {
+          const int o = (fy + 1) * RX + (cx + 2);  // region index of cell (gi, g)
+          auto B = [&](int var, int dxo, int dyo) { return double(W[var * PL + o + dxo + dyo * RX]); };
+          const double odx = 1.0 / a.dx;
+          const double eta_dx = eta_at(a.eta_kind, a.xc[gi], a.yc[g] + 0.5 * a.dx, 0.0) * odx;
+          const double JxS = eta_dx * (B(BZ, 0, 1) - B(BZ, 0, 0));
+          const double JzS = eta_dx * (0.25 * (B(BY, 1, 1) + B(BY, 1, 0) - B(BY, -1, 1) - B(BY, -1, 0)) -
+                                       (B(BX, 0, 1) - B(BX, 0, 0)));
+          F[EN] = F[EN] + 0.5 * (JzS * (B(BX, 0, 0) + B(BX, 0, 1)) - JxS * (B(BZ, 0, 0) + B(BZ, 0, 1)));
+          F[BX] = F[BX] + JzS;
+          F[BZ] = F[BZ] - JxS;
+        }
+      }
+    }
+    double* dst = xd ? m.FX + fb * m.fxr + fa : m.FY + fb * TX + fa;
+    const int dv = xd ? m.fxv : m.fyv;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) dst[k * dv] = F[k];
+  }
+}
+
 // phase C: fluxes of all x faces (work items 0..NXFP-1, padded to whole
 // warps) and all y faces (items NXFP..NXFP+NYF-1)
 template <class T, int FLUX, class G, int TAPE>
 __device__ __forceinline__ void phase_flux(const StageArgs& a, int bxi, int byi, const TileMem<T>& m, int t, int n,
                                            double chd) {
+  if constexpr (OMHD_FAST && sizeof(T) == 8) {
+    phase_flux_rot<T, FLUX, G, TAPE>(a, bxi, byi, m, t, n, chd);
+    return;
+  }
   constexpr int TX = G::TX, RX = G::RX;
   constexpr int NXS = G::NXS, NYS = G::NYS, NXF = G::NXF, NYF = G::NYF, NXFP = G::NXFP, XS = TX + 2;
   constexpr int PL = RX * G::RY;
