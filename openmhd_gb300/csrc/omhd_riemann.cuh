@@ -265,7 +265,7 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   // FAST FP64 forms of HLLD (fewer FP64-pipe operations, same mathematics):
   // the fast speeds compared by cross-multiplication and the larger taken as
   // sqrt(num / (2 rho)) in one rsqrt refinement; a*U - F formed once per side
-  // for the HLL average and the intermediate-state fluxes
+  // for the HLL average
   constexpr bool kF64 = FAST && sizeof(T) == 8;
   constexpr bool kRatio = kF64 && TYPE == FX_HLLD;
 
@@ -519,15 +519,21 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
             sR ? R[bt1] : L[bt1], sR ? R[bt2] : L[bt2], sR ? aR : aL, sR ? UR[EN] : UL[EN], sR ? ptR : ptL,
             sR ? vBR : vBL, sR ? roR : roL, sR ? ieR : ieL, aM, pt, Bn, S1, vs1, vs2);
         const T as = sR ? aR : aL;
-        T gs[NV];
+        // the side's state (conserved MX..EN, primitive rho and B) and flux; the
+        // fluxes keep the a*(U* - U) + F form, which is F itself wherever U* = U
+        T Us[NV], Fs[NV];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) gs[v] = sR ? gR[v] : gL[v];
-        if (!cen) {  // F(L*) :514-519 / F(R*) :522-527: a*(U* - U) + F = a*U* - g
+        for (int v = MX; v <= EN; ++v) Us[v] = sR ? UR[v] : UL[v];
 #pragma unroll
-          for (int v = MX; v <= EN; ++v) Fo[v] = as * S1[v] - gs[v];
-          Fo[RO] = as * S1[RO] - gs[RO];
-          Fo[bt1] = as * S1[bt1] - gs[bt1];
-          Fo[bt2] = as * S1[bt2] - gs[bt2];
+        for (int v = RO; v < NV; ++v) Us[v] = sR ? R[v] : L[v];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) Fs[v] = sR ? FR[v] : FL[v];
+        if (!cen) {  // F(L*) :514-519 / F(R*) :522-527
+#pragma unroll
+          for (int v = MX; v <= EN; ++v) Fo[v] = as * (S1[v] - Us[v]) + Fs[v];
+          Fo[RO] = as * (S1[RO] - Us[RO]) + Fs[RO];
+          Fo[bt1] = as * (S1[bt1] - Us[bt1]) + Fs[bt1];
+          Fo[bt2] = as * (S1[bt2] - Us[bt2]) + Fs[bt2];
         } else {  // central states :533-572
           T O1[NV] = {}, vo1, vo2;
           star_state<T, FAST, vn, vt1, vt2, bt1, bt2, mn, mt1, mt2>(
@@ -551,10 +557,10 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
           U2[mt2] = ros * at2;
           const T as1 = sR ? aR1 : aL1;
 #pragma unroll
-          for (int v = MX; v <= EN; ++v) Fo[v] = as1 * U2[v] - (as1 - as) * S1[v] - gs[v];
-          Fo[RO] = as1 * U2[RO] - (as1 - as) * S1[RO] - gs[RO];
-          Fo[bt1] = as1 * U2[bt1] - (as1 - as) * S1[bt1] - gs[bt1];
-          Fo[bt2] = as1 * U2[bt2] - (as1 - as) * S1[bt2] - gs[bt2];
+          for (int v = MX; v <= EN; ++v) Fo[v] = as1 * U2[v] - (as1 - as) * S1[v] - as * Us[v] + Fs[v];
+          Fo[RO] = as1 * U2[RO] - (as1 - as) * S1[RO] - as * Us[RO] + Fs[RO];
+          Fo[bt1] = as1 * U2[bt1] - (as1 - as) * S1[bt1] - as * Us[bt1] + Fs[bt1];
+          Fo[bt2] = as1 * U2[bt2] - (as1 - as) * S1[bt2] - as * Us[bt2] + Fs[bt2];
         }
       } else {
         // Region first (aL1, aR1 need only aM and the Alfven speeds), then the
@@ -598,34 +604,18 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
           UR1[mt2] = roR * vt2R;
         }
         if (sLs) {  // F(L*) :514-519
-          if constexpr (kF64) {  // aL*(UL1 - UL) + FL = aL*UL1 - gL
 #pragma unroll
-            for (int v = MX; v <= EN; ++v) Fo[v] = aL * UL1[v] - gL[v];
-            Fo[RO] = aL * UL1[RO] - gL[RO];
-            Fo[bt1] = aL * UL1[bt1] - gL[bt1];
-            Fo[bt2] = aL * UL1[bt2] - gL[bt2];
-          } else {
+          for (int v = MX; v <= EN; ++v) Fo[v] = aL * (UL1[v] - UL[v]) + FL[v];
+          Fo[RO] = aL * (UL1[RO] - L[RO]) + FL[RO];
+          Fo[bt1] = aL * (UL1[bt1] - L[bt1]) + FL[bt1];
+          Fo[bt2] = aL * (UL1[bt2] - L[bt2]) + FL[bt2];
+                } else if (sRs) {  // F(R*) :522-527
 #pragma unroll
-            for (int v = MX; v <= EN; ++v) Fo[v] = aL * (UL1[v] - UL[v]) + FL[v];
-            Fo[RO] = aL * (UL1[RO] - L[RO]) + FL[RO];
-            Fo[bt1] = aL * (UL1[bt1] - L[bt1]) + FL[bt1];
-            Fo[bt2] = aL * (UL1[bt2] - L[bt2]) + FL[bt2];
-          }
-        } else if (sRs) {  // F(R*) :522-527
-          if constexpr (kF64) {
-#pragma unroll
-            for (int v = MX; v <= EN; ++v) Fo[v] = aR * UR1[v] - gR[v];
-            Fo[RO] = aR * UR1[RO] - gR[RO];
-            Fo[bt1] = aR * UR1[bt1] - gR[bt1];
-            Fo[bt2] = aR * UR1[bt2] - gR[bt2];
-          } else {
-#pragma unroll
-            for (int v = MX; v <= EN; ++v) Fo[v] = aR * (UR1[v] - UR[v]) + FR[v];
-            Fo[RO] = aR * (UR1[RO] - R[RO]) + FR[RO];
-            Fo[bt1] = aR * (UR1[bt1] - R[bt1]) + FR[bt1];
-            Fo[bt2] = aR * (UR1[bt2] - R[bt2]) + FR[bt2];
-          }
-        } else {  // central states :533-572
+          for (int v = MX; v <= EN; ++v) Fo[v] = aR * (UR1[v] - UR[v]) + FR[v];
+          Fo[RO] = aR * (UR1[RO] - R[RO]) + FR[RO];
+          Fo[bt1] = aR * (UR1[bt1] - R[bt1]) + FR[bt1];
+          Fo[bt2] = aR * (UR1[bt2] - R[bt2]) + FR[bt2];
+                } else {  // central states :533-572
           T U2[NV];
           const T roLs = (FAST && sizeof(T) == 8) ? roL * rsL : sqrt(roL);
           const T roRs = (FAST && sizeof(T) == 8) ? roR * rsR : sqrt(roR);
@@ -641,39 +631,23 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
             U2[mn] = roL * aM;
             U2[mt1] = roL * at1;
             U2[mt2] = roL * at2;
-            if constexpr (kF64) {
 #pragma unroll
-              for (int v = MX; v <= EN; ++v) Fo[v] = aL1 * U2[v] - (aL1 - aL) * UL1[v] - gL[v];
-              Fo[RO] = aL1 * U2[RO] - (aL1 - aL) * UL1[RO] - gL[RO];
-              Fo[bt1] = aL1 * U2[bt1] - (aL1 - aL) * UL1[bt1] - gL[bt1];
-              Fo[bt2] = aL1 * U2[bt2] - (aL1 - aL) * UL1[bt2] - gL[bt2];
-            } else {
-#pragma unroll
-              for (int v = MX; v <= EN; ++v) Fo[v] = aL1 * U2[v] - (aL1 - aL) * UL1[v] - aL * UL[v] + FL[v];
-              Fo[RO] = aL1 * U2[RO] - (aL1 - aL) * UL1[RO] - aL * L[RO] + FL[RO];
-              Fo[bt1] = aL1 * U2[bt1] - (aL1 - aL) * UL1[bt1] - aL * L[bt1] + FL[bt1];
-              Fo[bt2] = aL1 * U2[bt2] - (aL1 - aL) * UL1[bt2] - aL * L[bt2] + FL[bt2];
-            }
-          } else {  // F(R**)
+            for (int v = MX; v <= EN; ++v) Fo[v] = aL1 * U2[v] - (aL1 - aL) * UL1[v] - aL * UL[v] + FL[v];
+            Fo[RO] = aL1 * U2[RO] - (aL1 - aL) * UL1[RO] - aL * L[RO] + FL[RO];
+            Fo[bt1] = aL1 * U2[bt1] - (aL1 - aL) * UL1[bt1] - aL * L[bt1] + FL[bt1];
+            Fo[bt2] = aL1 * U2[bt2] - (aL1 - aL) * UL1[bt2] - aL * L[bt2] + FL[bt2];
+                    } else {  // F(R**)
             U2[RO] = roR;
             U2[EN] = UR1[EN] + roRs * (vt1R * UR1[bt1] + vt2R * UR1[bt2] - at1 * U2[bt1] - at2 * U2[bt2]) * f2;
             U2[mn] = roR * aM;
             U2[mt1] = roR * at1;
             U2[mt2] = roR * at2;
-            if constexpr (kF64) {
 #pragma unroll
-              for (int v = MX; v <= EN; ++v) Fo[v] = aR1 * U2[v] - (aR1 - aR) * UR1[v] - gR[v];
-              Fo[RO] = aR1 * U2[RO] - (aR1 - aR) * UR1[RO] - gR[RO];
-              Fo[bt1] = aR1 * U2[bt1] - (aR1 - aR) * UR1[bt1] - gR[bt1];
-              Fo[bt2] = aR1 * U2[bt2] - (aR1 - aR) * UR1[bt2] - gR[bt2];
-            } else {
-#pragma unroll
-              for (int v = MX; v <= EN; ++v) Fo[v] = aR1 * U2[v] - (aR1 - aR) * UR1[v] - aR * UR[v] + FR[v];
-              Fo[RO] = aR1 * U2[RO] - (aR1 - aR) * UR1[RO] - aR * R[RO] + FR[RO];
-              Fo[bt1] = aR1 * U2[bt1] - (aR1 - aR) * UR1[bt1] - aR * R[bt1] + FR[bt1];
-              Fo[bt2] = aR1 * U2[bt2] - (aR1 - aR) * UR1[bt2] - aR * R[bt2] + FR[bt2];
-            }
-          }
+            for (int v = MX; v <= EN; ++v) Fo[v] = aR1 * U2[v] - (aR1 - aR) * UR1[v] - aR * UR[v] + FR[v];
+            Fo[RO] = aR1 * U2[RO] - (aR1 - aR) * UR1[RO] - aR * R[RO] + FR[RO];
+            Fo[bt1] = aR1 * U2[bt1] - (aR1 - aR) * UR1[bt1] - aR * R[bt1] + FR[bt1];
+            Fo[bt2] = aR1 * U2[bt2] - (aR1 - aR) * UR1[bt2] - aR * R[bt2] + FR[bt2];
+                    }
         }
       }
     }
