@@ -288,7 +288,7 @@ def run_ours(args):
                        "operands, best of five launches; nominal 1.25 TFLOP/s); MEASURED_PEAKS.json has no "
                        "FP64 entry",
         "flops_per_cell_update": flops_cu,
-        "kernel": "omhd::v_fp64::k_stage2d<double,HLLD,tape-capable>",
+        "kernel": "omhd::v_fp64::k_stage2d_pipe<HLLD,tape-capable,3 producer warps>",
         "hbm": {"achieved": hbm_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                 "frac": hbm_gbs / peaks.get("hbm_gbs", 1.0), "peak_source": peak_src,
                 "bytes_per_cell_update": BYTES_PER_CELL_UPDATE_2D},
