@@ -142,6 +142,42 @@ __device__ __forceinline__ double min_nonneg(double a, double b) {
   return (ib < ia) ? b : a;  // same operand choice as fmin2(a, b)
 }
 
+// The FAST minmod / MC reconstruction of reconstruct_fp64 from the slopes
+// gA = w0 - wm and gB = wp - w0 (computed once for two neighbouring cells,
+// whose gB and gA are the same difference); records the selection under
+// TAPE = tape::kRecord
+template <int TAPE = tape::kNone>
+__device__ __forceinline__ void reconstruct_fp64_g(int type, double gA, double gB, double wm, double w0, double wp,
+                                                   double& left, double& right, unsigned char* code = nullptr) {
+  const long long sa = __double_as_longlong(gA), sb = __double_as_longlong(gB);
+  const long long ia = __double_as_longlong(fabs(gA)), ib = __double_as_longlong(fabs(gB));
+  double m = min_nonneg(fabs(gA), fabs(gB));
+  double c = 0.5;  // minmod: (0.25 + 0.25)
+  bool pickC = false;
+  double gC = 0.0;
+  if (type == LM_MC) {
+    gC = 0.25 * (wp - wm);
+    const long long ic = __double_as_longlong(fabs(gC));
+    pickC = ic < __double_as_longlong(m);
+    m = min_nonneg(m, fabs(gC));
+    c = 1.0;  // MC: (0.5 + 0.5)
+  }
+  const bool zero = (sa ^ sb) < 0;
+  const double s = zero ? 0.0 : copysign(c, gA);
+  left = fma(s, m, w0);
+  right = fma(-s, m, w0);
+  if constexpr (TAPE == tape::kRecord) {
+    unsigned char k;
+    if (zero)
+      k = tape::kLimZero;
+    else if (pickC)
+      k = (unsigned char)(tape::kLimC | (((sa ^ __double_as_longlong(gC)) < 0) ? tape::kLimCNeg : 0));
+    else
+      k = (ib < ia) ? tape::kLimB : tape::kLimA;
+    *code = k;
+  }
+}
+
 // minmod and MC reconstruction for FP64 with the sign logic and the minimum
 // on the integer pipe.  (sign(c,gA)+sign(c,gB)) is 0 when the signs differ and
 // +-2c otherwise, and 2c*min(...) is an exact power-of-two scaling, so the face
@@ -174,35 +210,7 @@ __device__ __forceinline__ void reconstruct_fp64(int type, double wm, double w0,
   }
   if constexpr (FAST) {
     if (type == LM_MINMOD || type == LM_MC) {
-      const double gA = (w0 - wm);
-      const double gB = (wp - w0);
-      const long long sa = __double_as_longlong(gA), sb = __double_as_longlong(gB);
-      const long long ia = __double_as_longlong(fabs(gA)), ib = __double_as_longlong(fabs(gB));
-      double m = min_nonneg(fabs(gA), fabs(gB));
-      double c = 0.5;  // minmod: (0.25 + 0.25)
-      bool pickC = false;
-      double gC = 0.0;
-      if (type == LM_MC) {
-        gC = 0.25 * (wp - wm);
-        const long long ic = __double_as_longlong(fabs(gC));
-        pickC = ic < __double_as_longlong(m);
-        m = min_nonneg(m, fabs(gC));
-        c = 1.0;  // MC: (0.5 + 0.5)
-      }
-      const bool zero = (sa ^ sb) < 0;
-      const double s = zero ? 0.0 : copysign(c, gA);
-      left = fma(s, m, w0);
-      right = fma(-s, m, w0);
-      if constexpr (TAPE == tape::kRecord) {
-        unsigned char k;
-        if (zero)
-          k = tape::kLimZero;
-        else if (pickC)
-          k = (unsigned char)(tape::kLimC | (((sa ^ __double_as_longlong(gC)) < 0) ? tape::kLimCNeg : 0));
-        else
-          k = (ib < ia) ? tape::kLimB : tape::kLimA;
-        *code = k;
-      }
+      reconstruct_fp64_g<TAPE>(type, w0 - wm, wp - w0, wm, w0, wp, left, right, code);
       return;
     }
   }
