@@ -249,6 +249,200 @@ __device__ __forceinline__ void star_state(T ro, T un, T ut1, T ut2, T b1, T b2,
   S[mt2] = ros * v2;
 }
 
+// Per-side quantities of the FP64 HLLD solver (flux_solver.f90:359-401):
+// conserved normal momentum and energy, normal momentum flux, total
+// pressure, v.B and the numerator of the fast speed squared,
+// cf^2 = num / (2 rho).
+struct HSide {
+  double B2, vB, Umn, UE, Fmn, pt, num;
+};
+
+template <int DIR, int TAPE>
+__device__ __forceinline__ HSide hlld_side(const double (&S)[NV], double gamma, double r1, unsigned* code,
+                                           unsigned clamp_bit) {
+  constexpr int vn = VX + (DIR - 1) % 3, bn = BX + (DIR - 1) % 3;
+  HSide o;
+  const double v2 = S[VX] * S[VX] + S[VY] * S[VY] + S[VZ] * S[VZ];
+  o.B2 = S[BX] * S[BX] + S[BY] * S[BY] + S[BZ] * S[BZ];
+  o.vB = S[VX] * S[BX] + S[VY] * S[BY] + S[VZ] * S[BZ];
+  o.Umn = S[RO] * S[vn];
+  o.UE = 0.5 * (S[RO] * v2 + o.B2) + r1 * S[PR];
+  o.pt = S[PR] + 0.5 * o.B2;
+  o.Fmn = o.Umn * S[vn] + o.pt - S[bn] * S[bn];  // rho vn^2 + pt - bn^2
+  const double f1 = gamma * S[PR], f2 = 4 * (S[bn] * S[bn]);
+  const double D = (f1 + o.B2) * (f1 + o.B2) - f1 * f2;
+  const bool cl = tape::decide<TAPE>(lt0_<double, true>(D), code, clamp_bit);  // fmax2(D, 0)
+  o.num = (f1 + o.B2) + sqrt_nr(cl ? 0.0 : D);
+  return o;
+}
+
+// the physical flux of one side from its primitive state and HSide values
+template <int DIR>
+__device__ __forceinline__ void hlld_phys_flux(const double (&S)[NV], const HSide& h, double (&F)[NV]) {
+  constexpr int vn = VX + (DIR - 1) % 3, vt1 = VX + DIR % 3, vt2 = VX + (DIR + 1) % 3;
+  constexpr int bn = BX + (DIR - 1) % 3, bt1 = BX + DIR % 3, bt2 = BX + (DIR + 1) % 3;
+  constexpr int mn = MX + (DIR - 1) % 3, mt1 = MX + DIR % 3, mt2 = MX + (DIR + 1) % 3;
+  F[RO] = h.Umn;
+  F[mn] = h.Fmn;
+  F[mt1] = h.Umn * S[vt1] - S[bn] * S[bt1];
+  F[mt2] = h.Umn * S[vt2] - S[bn] * S[bt2];
+  F[EN] = (h.UE + h.pt) * S[vn] - h.vB * S[bn];  // (E + pt) vn - (v.B) bn
+  F[bt1] = S[vn] * S[bt1] - S[bn] * S[vt1];
+  F[bt2] = S[vn] * S[bt2] - S[bn] * S[vt2];
+  F[bn] = 0.0;
+  F[PS] = 0.0;
+}
+
+// HLLD flux of the FAST FP64 variant (flux_solver.f90:352-585, HLLC-G
+// fallback :447-476, GLM fluxes :580-581).  Same mathematics and decisions as
+// riemann_flux<double, DIR, FX_HLLD>; its work is cut to what the face's
+// region uses: per side only the quantities both sides need (the conserved
+// normal momentum and energy, the normal momentum flux, total pressure and
+// the fast-speed numerator); the HLL average only for rho, the normal momentum
+// and Bn (the tangential components serve the HLLC-G fallback alone); the
+// physical flux and the star state of the side s the region uses, from
+// side-selected inputs (the central region adds the other side's star state).
+template <int DIR, int TAPE>
+__device__ __forceinline__ void hlld_f64(const double (&L)[NV], const double (&R)[NV], double ch, double gamma,
+                                         double r1, double r2, double (&Fo)[NV], unsigned* code_io) {
+  using tape::decide;
+  unsigned code_reg = (TAPE == tape::kReplay) ? *code_io : 0u;
+  unsigned* const code = &code_reg;
+  constexpr int vn = VX + (DIR - 1) % 3, vt1 = VX + DIR % 3, vt2 = VX + (DIR + 1) % 3;
+  constexpr int bn = BX + (DIR - 1) % 3, bt1 = BX + DIR % 3, bt2 = BX + (DIR + 1) % 3;
+  constexpr int mn = MX + (DIR - 1) % 3, mt1 = MX + DIR % 3, mt2 = MX + (DIR + 1) % 3;
+  (void)r2;
+  const HSide hL = hlld_side<DIR, TAPE>(L, gamma, r1, code, tape::kClampL);
+  const HSide hR = hlld_side<DIR, TAPE>(R, gamma, r1, code, tape::kClampR);
+  // largest fast speed: cf^2 = num / (2 rho), numL/rhoL < numR/rhoR <=> numL*rhoR < numR*rhoL
+  const bool sr = decide<TAPE>(lt_<double, true>(hL.num * R[RO], hR.num * L[RO]), code, tape::kArSel);
+  const double cf = sqrt_ratio_<double, true>(sr ? hR.num : hL.num, 2 * (sr ? R[RO] : L[RO]));
+  const double aL = (decide<TAPE>(lt_<double, true>(R[vn], L[vn]), code, tape::kMinR) ? R[vn] : L[vn]) - cf;
+  const double aR = (decide<TAPE>(lt_<double, true>(L[vn], R[vn]), code, tape::kMaxR) ? R[vn] : L[vn]) + cf;
+  if (decide<TAPE>(ge0_<double, true>(aL), code, tape::kFL)) {
+    hlld_phys_flux<DIR>(L, hL, Fo);
+  } else if (decide<TAPE>(le0_<double, true>(aR), code, tape::kFR)) {
+    hlld_phys_flux<DIR>(R, hR, Fo);
+  } else {
+    // HLL average (:408-417) of rho, the normal momentum and Bn
+    const double f1 = rcp_nr(aR - aL);
+    const double tL = aL - L[vn], tR = aR - R[vn];
+    const double rtL = L[RO] * tL, rtR = R[RO] * tR;  // rho (a - vn) = a*rho - F[rho]
+    const double UhRO = f1 * (rtR - rtL);
+    const double Uhmn = f1 * ((aR * hR.Umn - hR.Fmn) - (aL * hL.Umn - hL.Fmn));
+    const double Ubn = f1 * (aR * R[bn] - aL * L[bn]);
+    const double aM = Uhmn * rcp_nr(UhRO);
+    const double pt = hL.pt + rtL * (aM - L[vn]);
+    const double ieL = rcp_nr(aL - aM), ieR = rcp_nr(aR - aM);
+    const double roL = rtL * ieL, roR = rtR * ieR;
+    const double rsL = rsqrt_nr(roL), rsR = rsqrt_nr(roR);
+    const bool bneg = decide<TAPE>(signbit(Ubn) != 0, code, tape::kBnNeg);
+    const double aBn = (TAPE == tape::kNone) ? fabs(Ubn) : (bneg ? -Ubn : Ubn);
+    const double aVL = aBn * rsL, aVR = aBn * rsR;
+    const double hllg = 1.001;
+    if (decide<TAPE>(!lt_<double, true>(aL, aM - hllg * aVL) || !lt_<double, true>(aM + hllg * aVR, aR), code,
+                     tape::kG)) {
+      // HLLC-G fallback :450-476 (rare): the tangential HLL components and
+      // both physical fluxes
+      double FL[NV], FR[NV];
+      hlld_phys_flux<DIR>(L, hL, FL);
+      hlld_phys_flux<DIR>(R, hR, FR);
+      const double ULt1 = L[RO] * L[vt1], ULt2 = L[RO] * L[vt2], URt1 = R[RO] * R[vt1], URt2 = R[RO] * R[vt2];
+      const double Uhmt1 = f1 * (aR * URt1 - aL * ULt1 - FR[mt1] + FL[mt1]);
+      const double Uhmt2 = f1 * (aR * URt2 - aL * ULt2 - FR[mt2] + FL[mt2]);
+      const double Uhbt1 = f1 * (aR * R[bt1] - aL * L[bt1] - FR[bt1] + FL[bt1]);
+      const double Uhbt2 = f1 * (aR * R[bt2] - aL * L[bt2] - FR[bt2] + FL[bt2]);
+      const double f2 = aL * aR;
+      Fo[bt1] = f1 * (aR * FL[bt1] - aL * FR[bt1] + f2 * (R[bt1] - L[bt1]));
+      Fo[bt2] = f1 * (aR * FL[bt2] - aL * FR[bt2] + f2 * (R[bt2] - L[bt2]));
+      const double iUr = rcp_nr(UhRO);
+      const double at1 = Uhmt1 * iUr, at2 = Uhmt2 * iUr;
+      const double enL = ((aL - L[vn]) * hL.UE - hL.pt * L[vn] + pt * aM +
+                          Ubn * (hL.vB - aM * Ubn - at1 * Uhbt1 - at2 * Uhbt2)) * ieL;
+      const double enR = ((aR - R[vn]) * hR.UE - hR.pt * R[vn] + pt * aM +
+                          Ubn * (hR.vB - aM * Ubn - at1 * Uhbt1 - at2 * Uhbt2)) * ieR;
+      const double g1 = (TAPE != tape::kNone) ? (decide<TAPE>(signbit(aM) == 0, code, tape::kGLeft) ? 1.0 : 0.0)
+                                              : 0.5 + fsign(0.5, aM);  // 0.5 + sign(0.5, aM)
+      const double g2 = 1.0 - g1;
+      Fo[mn] = g1 * (aL * (roL * aM - hL.Umn) + FL[mn]) + g2 * (aR * (roR * aM - hR.Umn) + FR[mn]);
+      Fo[mt1] = g1 * (aL * (roL * at1 - ULt1) + FL[mt1]) + g2 * (aR * (roR * at1 - URt1) + FR[mt1]);
+      Fo[mt2] = g1 * (aL * (roL * at2 - ULt2) + FL[mt2]) + g2 * (aR * (roR * at2 - URt2) + FR[mt2]);
+      Fo[EN] = g1 * (aL * (enL - hL.UE) + FL[EN]) + g2 * (aR * (enR - hR.UE) + FR[EN]);
+      Fo[RO] = g1 * (aL * (roL - L[RO]) + FL[RO]) + g2 * (aR * (roR - R[RO]) + FR[RO]);
+    } else {
+      // region (:482-572), then the side s whose state the flux uses
+      const double aL1 = aM - aVL, aR1 = aM + aVR;
+      const bool sLs = decide<TAPE>(ge0_<double, true>(aL1), code, tape::kLS);
+      const bool sRs = !sLs && decide<TAPE>(le0_<double, true>(aR1), code, tape::kRS);
+      const bool cen = !sLs && !sRs;
+      const bool sR = sRs || (cen && !decide<TAPE>(ge0_<double, true>(aM), code, tape::kSSLeft));
+      double Ss[NV];  // side primitive state
+#pragma unroll
+      for (int v = 0; v < NV; ++v) Ss[v] = sR ? R[v] : L[v];
+      HSide hs;
+      hs.B2 = sR ? hR.B2 : hL.B2;
+      hs.vB = sR ? hR.vB : hL.vB;
+      hs.Umn = sR ? hR.Umn : hL.Umn;
+      hs.UE = sR ? hR.UE : hL.UE;
+      hs.Fmn = sR ? hR.Fmn : hL.Fmn;
+      hs.pt = sR ? hR.pt : hL.pt;
+      const double as = sR ? aR : aL;
+      double S1[NV] = {}, vs1, vs2;
+      star_state<double, true, vn, vt1, vt2, bt1, bt2, mn, mt1, mt2>(
+          Ss[RO], Ss[vn], Ss[vt1], Ss[vt2], Ss[bt1], Ss[bt2], as, hs.UE, hs.pt, hs.vB, sR ? roR : roL,
+          sR ? ieR : ieL, aM, pt, Ubn, S1, vs1, vs2);
+      double Fs[NV], Us[NV];  // the side's physical flux and state (conserved MX..EN, primitive rho and B)
+      hlld_phys_flux<DIR>(Ss, hs, Fs);
+      Us[mn] = hs.Umn;
+      Us[mt1] = Ss[RO] * Ss[vt1];
+      Us[mt2] = Ss[RO] * Ss[vt2];
+      Us[EN] = hs.UE;
+      Us[RO] = Ss[RO];
+      Us[bt1] = Ss[bt1];
+      Us[bt2] = Ss[bt2];
+      if (!cen) {  // F(L*) :514-519 / F(R*) :522-527
+#pragma unroll
+        for (int v = MX; v <= EN; ++v) Fo[v] = as * (S1[v] - Us[v]) + Fs[v];
+        Fo[RO] = as * (S1[RO] - Us[RO]) + Fs[RO];
+        Fo[bt1] = as * (S1[bt1] - Us[bt1]) + Fs[bt1];
+        Fo[bt2] = as * (S1[bt2] - Us[bt2]) + Fs[bt2];
+      } else {  // central states :533-572, symmetric in (s, o); sigma = +1 for s = L, -1 for s = R
+        double O1[NV] = {}, vo1, vo2;
+        star_state<double, true, vn, vt1, vt2, bt1, bt2, mn, mt1, mt2>(
+            sR ? L[RO] : R[RO], sR ? L[vn] : R[vn], sR ? L[vt1] : R[vt1], sR ? L[vt2] : R[vt2],
+            sR ? L[bt1] : R[bt1], sR ? L[bt2] : R[bt2], sR ? aL : aR, sR ? hL.UE : hR.UE, sR ? hL.pt : hR.pt,
+            sR ? hL.vB : hR.vB, sR ? roL : roR, sR ? ieL : ieR, aM, pt, Ubn, O1, vo1, vo2);
+        const double ros = sR ? roR : roL, roo = sR ? roL : roR;
+        const double rss = ros * (sR ? rsR : rsL), rso = roo * (sR ? rsL : rsR);  // sqrt(rho*) of s and o
+        const double fc = rcp_nr(rss + rso);
+        const double f2 = (TAPE == tape::kNone) ? fsign(1.0, Ubn) : (bneg ? -1.0 : 1.0);
+        const double f2s = sR ? -f2 : f2;
+        double U2[NV];
+        const double at1 = fc * (rss * vs1 + rso * vo1 + (O1[bt1] - S1[bt1]) * f2s);
+        const double at2 = fc * (rss * vs2 + rso * vo2 + (O1[bt2] - S1[bt2]) * f2s);
+        U2[bt1] = fc * (rss * O1[bt1] + rso * S1[bt1] + rss * rso * (vo1 - vs1) * f2s);
+        U2[bt2] = fc * (rss * O1[bt2] + rso * S1[bt2] + rss * rso * (vo2 - vs2) * f2s);
+        U2[RO] = ros;
+        U2[EN] = S1[EN] - rss * (vs1 * S1[bt1] + vs2 * S1[bt2] - at1 * U2[bt1] - at2 * U2[bt2]) * f2s;
+        U2[mn] = ros * aM;
+        U2[mt1] = ros * at1;
+        U2[mt2] = ros * at2;
+        const double as1 = sR ? aR1 : aL1;
+#pragma unroll
+        for (int v = MX; v <= EN; ++v) Fo[v] = as1 * U2[v] - (as1 - as) * S1[v] - as * Us[v] + Fs[v];
+        Fo[RO] = as1 * U2[RO] - (as1 - as) * S1[RO] - as * Us[RO] + Fs[RO];
+        Fo[bt1] = as1 * U2[bt1] - (as1 - as) * S1[bt1] - as * Us[bt1] + Fs[bt1];
+        Fo[bt2] = as1 * U2[bt2] - (as1 - as) * S1[bt2] - as * Us[bt2] + Fs[bt2];
+      }
+    }
+  }
+  // GLM fluxes :580-581, the halving folded into the (exact) half speeds
+  const double hch = 0.5 * ch, hch2 = 0.5 * (ch * ch);
+  Fo[bn] = 0.5 * (L[PS] + R[PS]) - hch * (R[bn] - L[bn]);
+  Fo[PS] = hch2 * (L[bn] + R[bn]) - hch * (R[PS] - L[PS]);
+  if constexpr (TAPE == tape::kRecord) *code_io = code_reg;
+}
+
 // Numerical flux across one face (2D_basic/flux_solver.f90):
 //   LLF :89-148, HLL :153-221, HLLC :226-347, HLLD :352-585 (HLLC-G fallback
 //   :447-476), LHLLD :590-789; GLM fluxes for Bn and psi :580-581.
@@ -261,6 +455,10 @@ template <class T, int DIR, int TYPE, bool FAST = false, int TAPE = tape::kNone>
 __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV], T ch, T gamma, T r1,
                                              T r2, T (&Fo)[NV], unsigned* code_io = nullptr) {
   using tape::decide;
+  if constexpr (FAST && sizeof(T) == 8 && TYPE == FX_HLLD) {
+    hlld_f64<DIR, TAPE>(L, R, ch, gamma, r1, r2, Fo, code_io);
+    return;
+  }
   // the face's decision word lives in a register here; read from / written to
   // *code_io once (replay / record)
   unsigned code_reg = (TAPE == tape::kReplay) ? *code_io : 0u;
@@ -270,12 +468,6 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   constexpr int mn = MX + (DIR - 1) % 3, mt1 = MX + DIR % 3, mt2 = MX + (DIR + 1) % 3;
   const T hllg_factor = T(1.001);
   const T ch2 = ch * ch;
-  // FAST FP64 forms of HLLD (fewer FP64-pipe operations, same mathematics):
-  // the fast speeds compared by cross-multiplication and the larger taken as
-  // sqrt(num / (2 rho)) in one rsqrt refinement; a*U - F formed once per side
-  // for the HLL average
-  constexpr bool kF64 = FAST && sizeof(T) == 8;
-  constexpr bool kRatio = kF64 && TYPE == FX_HLLD;
 
   T UL[4], UR[4], FL[NV], FR[NV];
 #pragma unroll
@@ -295,14 +487,8 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   UL[MZ] = L[RO] * L[VZ];
   UL[EN] = T(0.5) * (L[RO] * v2 + B2) + r1 * L[PR];
   FL[RO] = L[RO] * L[vn];
-  if constexpr (kF64) {  // with pt = p + B^2/2: rho vn^2 + pt - bn^2 and (E + pt) vn - (v.B) bn (r2 = r1 + 1)
-    const T pt_ = L[PR] + T(0.5) * B2;
-    FL[mn] = UL[mn] * L[vn] + pt_ - L[bn] * L[bn];
-    FL[EN] = (UL[EN] + pt_) * L[vn] - vBL * L[bn];
-  } else {
-    FL[mn] = L[RO] * L[vn] * L[vn] - L[bn] * L[bn] + L[PR] + T(0.5) * B2;
-    FL[EN] = (T(0.5) * L[RO] * v2 + r2 * L[PR] + B2) * L[vn] - vBL * L[bn];
-  }
+  FL[mn] = L[RO] * L[vn] * L[vn] - L[bn] * L[bn] + L[PR] + T(0.5) * B2;
+  FL[EN] = (T(0.5) * L[RO] * v2 + r2 * L[PR] + B2) * L[vn] - vBL * L[bn];
   FL[mt1] = L[RO] * L[vn] * L[vt1] - L[bn] * L[bt1];
   FL[mt2] = L[RO] * L[vn] * L[vt2] - L[bn] * L[bt2];
   FL[bt1] = L[vn] * L[bt1] - L[bn] * L[vt1];
@@ -315,8 +501,7 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
     {  // fmax2(D, 0)
       const T D = (f1 + B2) * (f1 + B2) - f1 * f2;
       const bool cl = decide<TAPE>(lt0_<T, FAST>(D), code, tape::kClampL);
-      const T num = (f1 + B2) + sqrt_<T, FAST>(cl ? T(0) : D);
-      aL = kRatio ? num : div_<T, FAST>(num, 2 * L[RO]);  // kRatio: numerator of cf^2
+      aL = div_<T, FAST>((f1 + B2) + sqrt_<T, FAST>(cl ? T(0) : D), 2 * L[RO]);
     }
     ptL = L[PR] + T(0.5) * B2;
     if (TYPE == FX_LHLLD) {
@@ -334,14 +519,8 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   UR[MZ] = R[RO] * R[VZ];
   UR[EN] = T(0.5) * (R[RO] * v2 + B2) + r1 * R[PR];
   FR[RO] = R[RO] * R[vn];
-  if constexpr (kF64) {  // with pt = p + B^2/2: rho vn^2 + pt - bn^2 and (E + pt) vn - (v.B) bn (r2 = r1 + 1)
-    const T pt_ = R[PR] + T(0.5) * B2;
-    FR[mn] = UR[mn] * R[vn] + pt_ - R[bn] * R[bn];
-    FR[EN] = (UR[EN] + pt_) * R[vn] - vBR * R[bn];
-  } else {
-    FR[mn] = R[RO] * R[vn] * R[vn] - R[bn] * R[bn] + R[PR] + T(0.5) * B2;
-    FR[EN] = (T(0.5) * R[RO] * v2 + r2 * R[PR] + B2) * R[vn] - vBR * R[bn];
-  }
+  FR[mn] = R[RO] * R[vn] * R[vn] - R[bn] * R[bn] + R[PR] + T(0.5) * B2;
+  FR[EN] = (T(0.5) * R[RO] * v2 + r2 * R[PR] + B2) * R[vn] - vBR * R[bn];
   FR[mt1] = R[RO] * R[vn] * R[vt1] - R[bn] * R[bt1];
   FR[mt2] = R[RO] * R[vn] * R[vt2] - R[bn] * R[bt2];
   FR[bt1] = R[vn] * R[bt1] - R[bn] * R[vt1];
@@ -354,8 +533,7 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
     {  // fmax2(D, 0)
       const T D = (f1 + B2) * (f1 + B2) - f1 * f2;
       const bool cl = decide<TAPE>(lt0_<T, FAST>(D), code, tape::kClampR);
-      const T num = (f1 + B2) + sqrt_<T, FAST>(cl ? T(0) : D);
-      aR = kRatio ? num : div_<T, FAST>(num, 2 * R[RO]);  // kRatio: numerator of cf^2
+      aR = div_<T, FAST>((f1 + B2) + sqrt_<T, FAST>(cl ? T(0) : D), 2 * R[RO]);
     }
     ptR = R[PR] + T(0.5) * B2;
     if (TYPE == FX_LHLLD) {
@@ -419,12 +597,7 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
       f1 = fmin2(T(1), div_<T, FAST>(fmax2(aL1, aR1), fmax2(aL, aR)));
       psi = 2 * sqrt(f1) - f1;
     }
-    if constexpr (kRatio) {  // cf^2 = num / (2 rho): numL/rhoL < numR/rhoR <=> numL*rhoR < numR*rhoL
-      const bool sr = decide<TAPE>(lt_<T, FAST>(aL * R[RO], aR * L[RO]), code, tape::kArSel);
-      f1 = sqrt_ratio_<T, FAST>(sr ? aR : aL, 2 * (sr ? R[RO] : L[RO]));
-    } else {
-      f1 = sqrt_<T, FAST>(decide<TAPE>(lt_<T, FAST>(aL, aR), code, tape::kArSel) ? aR : aL);  // fmax2(aL, aR)
-    }
+    f1 = sqrt_<T, FAST>(decide<TAPE>(lt_<T, FAST>(aL, aR), code, tape::kArSel) ? aR : aL);  // fmax2(aL, aR)
     aL = (decide<TAPE>(lt_<T, FAST>(R[vn], L[vn]), code, tape::kMinR) ? R[vn] : L[vn]) - f1;  // fmin2
     aR = (decide<TAPE>(lt_<T, FAST>(L[vn], R[vn]), code, tape::kMaxR) ? R[vn] : L[vn]) + f1;  // fmax2
     if (decide<TAPE>(ge0_<T, FAST>(aL), code, tape::kFL)) {
@@ -434,28 +607,12 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
 #pragma unroll
       for (int v = 0; v < NV; ++v) Fo[v] = FR[v];
     } else {
-      T Uh[NV], gL[NV] = {}, gR[NV] = {};
+      T Uh[NV];
       f1 = rcp_<T, FAST>(aR - aL);
-      if constexpr (kF64) {  // g = a*U - F per side (MX..BZ)
 #pragma unroll
-        for (int v = MX; v <= EN; ++v) {
-          gL[v] = aL * UL[v] - FL[v];
-          gR[v] = aR * UR[v] - FR[v];
-        }
+      for (int v = MX; v <= MZ; ++v) Uh[v] = f1 * (aR * UR[v] - aL * UL[v] - FR[v] + FL[v]);
 #pragma unroll
-        for (int v = RO; v <= BZ; ++v) {
-          gL[v] = aL * L[v] - FL[v];
-          gR[v] = aR * R[v] - FR[v];
-        }
-#pragma unroll
-        for (int v = MX; v <= BZ; ++v)
-          if (v != EN) Uh[v] = f1 * (gR[v] - gL[v]);
-      } else {
-#pragma unroll
-        for (int v = MX; v <= MZ; ++v) Uh[v] = f1 * (aR * UR[v] - aL * UL[v] - FR[v] + FL[v]);
-#pragma unroll
-        for (int v = RO; v <= BZ; ++v) Uh[v] = f1 * (aR * R[v] - aL * L[v] - FR[v] + FL[v]);
-      }
+      for (int v = RO; v <= BZ; ++v) Uh[v] = f1 * (aR * R[v] - aL * L[v] - FR[v] + FL[v]);
       const T aM = div_<T, FAST>(Uh[mn], Uh[RO]);
       T pt;
       if (TYPE == FX_LHLLD) {
@@ -504,72 +661,6 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
         Fo[mt2] = f1 * (aL * (roL * at2 - UL[mt2]) + FL[mt2]) + f2 * (aR * (roR * at2 - UR[mt2]) + FR[mt2]);
         Fo[EN] = f1 * (aL * (enL - UL[EN]) + FL[EN]) + f2 * (aR * (enR - UR[EN]) + FR[EN]);
         Fo[RO] = f1 * (aL * (roL - L[RO]) + FL[RO]) + f2 * (aR * (roR - R[RO]) + FR[RO]);
-      } else if constexpr (kF64) {
-        // Side-selected intermediate states (FAST FP64).  The region picks the
-        // side s whose state the flux uses (F(L*) and F(L**): L; F(R*) and
-        // F(R**): R); every lane builds the star state of its own side from
-        // selected inputs, so a warp whose faces take different sides runs one
-        // star-state computation, not both; the central states (both sides)
-        // add the other side's star state.  The L* and R* formulas of
-        // :482-507 are mirror images, so the selected inputs give them exactly;
-        // the central states :533-572 are written symmetrically in (s, o)
-        // with sigma = +1 for s = L and -1 for s = R: (UR1 - UL1) = sigma (O1 - S1).
-        aL1 = aM - aVL;
-        aR1 = aM + aVR;
-        const bool sLs = decide<TAPE>(ge0_<T, FAST>(aL1), code, tape::kLS);
-        const bool sRs = !sLs && decide<TAPE>(le0_<T, FAST>(aR1), code, tape::kRS);
-        const bool cen = !sLs && !sRs;
-        const bool sR = sRs || (cen && !decide<TAPE>(ge0_<T, FAST>(aM), code, tape::kSSLeft));
-        const T Bn = Uh[bn];
-        T S1[NV] = {}, vs1, vs2;
-        star_state<T, FAST, vn, vt1, vt2, bt1, bt2, mn, mt1, mt2>(
-            sR ? R[RO] : L[RO], sR ? R[vn] : L[vn], sR ? R[vt1] : L[vt1], sR ? R[vt2] : L[vt2],
-            sR ? R[bt1] : L[bt1], sR ? R[bt2] : L[bt2], sR ? aR : aL, sR ? UR[EN] : UL[EN], sR ? ptR : ptL,
-            sR ? vBR : vBL, sR ? roR : roL, sR ? ieR : ieL, aM, pt, Bn, S1, vs1, vs2);
-        const T as = sR ? aR : aL;
-        // the side's state (conserved MX..EN, primitive rho and B) and flux; the
-        // fluxes keep the a*(U* - U) + F form, which is F itself wherever U* = U
-        T Us[NV], Fs[NV];
-#pragma unroll
-        for (int v = MX; v <= EN; ++v) Us[v] = sR ? UR[v] : UL[v];
-#pragma unroll
-        for (int v = RO; v < NV; ++v) Us[v] = sR ? R[v] : L[v];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) Fs[v] = sR ? FR[v] : FL[v];
-        if (!cen) {  // F(L*) :514-519 / F(R*) :522-527
-#pragma unroll
-          for (int v = MX; v <= EN; ++v) Fo[v] = as * (S1[v] - Us[v]) + Fs[v];
-          Fo[RO] = as * (S1[RO] - Us[RO]) + Fs[RO];
-          Fo[bt1] = as * (S1[bt1] - Us[bt1]) + Fs[bt1];
-          Fo[bt2] = as * (S1[bt2] - Us[bt2]) + Fs[bt2];
-        } else {  // central states :533-572
-          T O1[NV] = {}, vo1, vo2;
-          star_state<T, FAST, vn, vt1, vt2, bt1, bt2, mn, mt1, mt2>(
-              sR ? L[RO] : R[RO], sR ? L[vn] : R[vn], sR ? L[vt1] : R[vt1], sR ? L[vt2] : R[vt2],
-              sR ? L[bt1] : R[bt1], sR ? L[bt2] : R[bt2], sR ? aL : aR, sR ? UL[EN] : UR[EN], sR ? ptL : ptR,
-              sR ? vBL : vBR, sR ? roL : roR, sR ? ieL : ieR, aM, pt, Bn, O1, vo1, vo2);
-          const T ros = sR ? roR : roL, roo = sR ? roL : roR;
-          const T rss = ros * (sR ? rsR : rsL), rso = roo * (sR ? rsL : rsR);  // sqrt(rho*) of s and o
-          f1 = rcp_<T, FAST>(rss + rso);
-          const T f2 = (TAPE == tape::kNone) ? fsign(T(1), Bn) : (bneg ? T(-1) : T(1));
-          const T f2s = sR ? -f2 : f2;
-          T U2[NV];
-          const T at1 = f1 * (rss * vs1 + rso * vo1 + (O1[bt1] - S1[bt1]) * f2s);
-          const T at2 = f1 * (rss * vs2 + rso * vo2 + (O1[bt2] - S1[bt2]) * f2s);
-          U2[bt1] = f1 * (rss * O1[bt1] + rso * S1[bt1] + rss * rso * (vo1 - vs1) * f2s);
-          U2[bt2] = f1 * (rss * O1[bt2] + rso * S1[bt2] + rss * rso * (vo2 - vs2) * f2s);
-          U2[RO] = ros;
-          U2[EN] = S1[EN] - rss * (vs1 * S1[bt1] + vs2 * S1[bt2] - at1 * U2[bt1] - at2 * U2[bt2]) * f2s;
-          U2[mn] = ros * aM;
-          U2[mt1] = ros * at1;
-          U2[mt2] = ros * at2;
-          const T as1 = sR ? aR1 : aL1;
-#pragma unroll
-          for (int v = MX; v <= EN; ++v) Fo[v] = as1 * U2[v] - (as1 - as) * S1[v] - as * Us[v] + Fs[v];
-          Fo[RO] = as1 * U2[RO] - (as1 - as) * S1[RO] - as * Us[RO] + Fs[RO];
-          Fo[bt1] = as1 * U2[bt1] - (as1 - as) * S1[bt1] - as * Us[bt1] + Fs[bt1];
-          Fo[bt2] = as1 * U2[bt2] - (as1 - as) * S1[bt2] - as * Us[bt2] + Fs[bt2];
-        }
       } else {
         // Region first (aL1, aR1 need only aM and the Alfven speeds), then the
         // intermediate states that region uses: F(L*) needs L* only, F(R*)
@@ -661,14 +752,8 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
     }
   }
   // GLM fluxes :580-581
-  if constexpr (kF64) {  // the halving folded into the (exact) half speeds
-    const T hch = T(0.5) * ch, hch2 = T(0.5) * ch2;
-    Fo[bn] = T(0.5) * (L[PS] + R[PS]) - hch * (R[bn] - L[bn]);
-    Fo[PS] = hch2 * (L[bn] + R[bn]) - hch * (R[PS] - L[PS]);
-  } else {
-    Fo[bn] = T(0.5) * ((L[PS] + R[PS]) - ch * (R[bn] - L[bn]));
-    Fo[PS] = T(0.5) * (ch2 * (L[bn] + R[bn]) - ch * (R[PS] - L[PS]));
-  }
+  Fo[bn] = T(0.5) * ((L[PS] + R[PS]) - ch * (R[bn] - L[bn]));
+  Fo[PS] = T(0.5) * (ch2 * (L[bn] + R[bn]) - ch * (R[PS] - L[PS]));
   if constexpr (TAPE == tape::kRecord) *code_io = code_reg;
 }
 
