@@ -240,15 +240,20 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
     for (int q = 0; q < 7; ++q) gsR.F[fl[q]] += gF[fl[q]];
   } else {
     const double ih = arcp(SR - SL);
+    // HLL state: rho, the normal momentum and Bn here; the tangential
+    // components only in the HLLC-G fallback, the one branch that uses them
     double NU[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, Uh[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int k = 0; k < 3; ++k) {
+    auto hll_m = [&](int k) {  // momentum components (conserved Um)
       NU[k] = SR * sR.Um[k] - SL * sL.Um[k] - sR.F[k] + sL.F[k];
       Uh[k] = ih * NU[k];
-    }
-    for (int k = kRO; k <= 7; ++k) {
+    };
+    auto hll_p = [&](int k) {  // rho and B (primitive = conserved)
       NU[k] = SR * R[k] - SL * L[k] - sR.F[k] + sL.F[k];
       Uh[k] = ih * NU[k];
-    }
+    };
+    hll_m(mn);
+    hll_p(kRO);
+    hll_p(bn);
     const double iUr = arcp(Uh[kRO]);
     const double aM = Uh[mn] * iUr;
     const double tL = SL - L[vn], tR = SR - R[vn];
@@ -267,8 +272,13 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
     double gih = 0.0, gaM = 0.0, gpts = 0.0, gtL = 0.0, gtR = 0.0, geL = 0.0, geR = 0.0;
     double groL = 0.0, groR = 0.0, gaVL = 0.0, gaVR = 0.0, gsqL = 0.0, gsqR = 0.0;
 
-    if (decide<MODE>((SL >= (aM - hf * aVL)) || ((aM + hf * aVR) >= SR), code, tape::kG)) {
+    const bool gbr = decide<MODE>((SL >= (aM - hf * aVL)) || ((aM + hf * aVR) >= SR), code, tape::kG);
+    if (gbr) {
       // ---- HLLC-G fallback (flux_solver.f90:450-476) ----
+      hll_m(mt1);
+      hll_m(mt2);
+      hll_p(bt1);
+      hll_p(bt2);
       const double f2g = SL * SR;
       double gf2g = 0.0;
       const int bts[2] = {bt1, bt2};
@@ -729,7 +739,7 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
     gR[vn] -= gtR;
     gUh[mn] += gaM * iUr;
     gUh[kRO] -= gaM * aM * iUr;
-    for (int k = 0; k < 3; ++k) {
+    auto hll_m_adj = [&](int k) {
       gih += gUh[k] * NU[k];
       const double gN = ih * gUh[k];
       gSR += gN * sR.Um[k];
@@ -738,8 +748,8 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
       gsL.Um[k] -= gN * SL;
       gsR.F[k] -= gN;
       gsL.F[k] += gN;
-    }
-    for (int k = kRO; k <= 7; ++k) {
+    };
+    auto hll_p_adj = [&](int k) {
       gih += gUh[k] * NU[k];
       const double gN = ih * gUh[k];
       gSR += gN * R[k];
@@ -748,6 +758,15 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
       gL[k] -= gN * SL;
       gsR.F[k] -= gN;
       gsL.F[k] += gN;
+    };
+    hll_m_adj(mn);
+    hll_p_adj(kRO);
+    hll_p_adj(bn);
+    if (gbr) {  // the tangential components carry gradient only there
+      hll_m_adj(mt1);
+      hll_m_adj(mt2);
+      hll_p_adj(bt1);
+      hll_p_adj(bt2);
     }
     gSR -= gih * ih * ih;
     gSL += gih * ih * ih;
