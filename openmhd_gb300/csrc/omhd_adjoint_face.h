@@ -75,11 +75,6 @@ OMHD_HD void side_fwd(const double* s, double gamma, double r1, double r2, Side&
   for (int k = 0; k < 9; ++k) o.F[k] = 0.0;
   o.F[kRO] = s[kRO] * s[vn];
   o.F[mn] = s[kRO] * s[vn] * s[vn] - s[bn] * s[bn] + s[kPR] + 0.5 * o.B2;
-  o.F[mt1] = s[kRO] * s[vn] * s[vt1] - s[bn] * s[bt1];
-  o.F[mt2] = s[kRO] * s[vn] * s[vt2] - s[bn] * s[bt2];
-  o.F[kEN] = (0.5 * s[kRO] * o.v2 + r2 * s[kPR] + o.B2) * s[vn] - o.vB * s[bn];
-  o.F[bt1] = s[vn] * s[bt1] - s[bn] * s[vt1];
-  o.F[bt2] = s[vn] * s[bt2] - s[bn] * s[vt2];
   o.f1 = gamma * s[kPR];
   o.f2 = 4 * (s[bn] * s[bn]);
   o.Q = o.f1 + o.B2;
@@ -92,9 +87,25 @@ OMHD_HD void side_fwd(const double* s, double gamma, double r1, double r2, Side&
   o.pt = s[kPR] + 0.5 * o.B2;
 }
 
+// the tangential momentum, energy and tangential field fluxes of one side
+// (flux_solver.f90:368-372): only the HLLC-G fallback reads their values
+template <int DIR>
+OMHD_HD void side_fwd_tan(const double* s, double r2, Side& o) {
+  constexpr int vn = (DIR - 1) % 3, vt1 = DIR % 3, vt2 = (DIR + 1) % 3;
+  constexpr int bn = kBX + (DIR - 1) % 3, bt1 = kBX + DIR % 3, bt2 = kBX + (DIR + 1) % 3;
+  constexpr int mt1 = vt1, mt2 = vt2;
+  o.F[mt1] = s[kRO] * s[vn] * s[vt1] - s[bn] * s[bt1];
+  o.F[mt2] = s[kRO] * s[vn] * s[vt2] - s[bn] * s[bt2];
+  o.F[kEN] = (0.5 * s[kRO] * o.v2 + r2 * s[kPR] + o.B2) * s[vn] - o.vB * s[bn];
+  o.F[bt1] = s[vn] * s[bt1] - s[bn] * s[vt1];
+  o.F[bt2] = s[vn] * s[bt2] - s[bn] * s[vt2];
+}
+
+// flux = false: the side's tangential momentum, energy and tangential field
+// fluxes carry no gradient (g.F is zero there), and their reverse is skipped
 template <int DIR>
 OMHD_HD void side_adj(const double* s, double gamma, double r1, double r2, const Side& o, const SideG& g,
-                      double* gs) {
+                      double* gs, bool flux = true) {
   constexpr int vn = (DIR - 1) % 3, vt1 = DIR % 3, vt2 = (DIR + 1) % 3;
   constexpr int bn = kBX + (DIR - 1) % 3, bt1 = kBX + DIR % 3, bt2 = kBX + (DIR + 1) % 3;
   constexpr int mn = vn, mt1 = vt1, mt2 = vt2;
@@ -116,50 +127,52 @@ OMHD_HD void side_adj(const double* s, double gamma, double r1, double r2, const
   gB2 += gQ;
   gB[bn - kBX] += 8 * s[bn] * gf2;
   gp += gamma * gf1;
-  // tangential field fluxes
-  {
-    const double q = g.F[bt2];
-    gv[vn] += q * s[bt2];
-    gB[bt2 - kBX] += q * s[vn];
-    gB[bn - kBX] -= q * s[vt2];
-    gv[vt2] -= q * s[bn];
-  }
-  {
-    const double q = g.F[bt1];
-    gv[vn] += q * s[bt1];
-    gB[bt1 - kBX] += q * s[vn];
-    gB[bn - kBX] -= q * s[vt1];
-    gv[vt1] -= q * s[bn];
-  }
-  // energy flux (K vn - vB bn)
-  {
-    const double q = g.F[kEN];
-    const double K = 0.5 * s[kRO] * o.v2 + r2 * s[kPR] + o.B2;
-    const double gK = q * s[vn];
-    gv[vn] += q * K;
-    gvB -= q * s[bn];
-    gB[bn - kBX] -= q * o.vB;
-    gro += 0.5 * o.v2 * gK;
-    gv2 += 0.5 * s[kRO] * gK;
-    gp += r2 * gK;
-    gB2 += gK;
-  }
-  // tangential momentum fluxes
-  {
-    const double q = g.F[mt2];
-    gro += q * s[vn] * s[vt2];
-    gv[vn] += q * s[kRO] * s[vt2];
-    gv[vt2] += q * s[kRO] * s[vn];
-    gB[bn - kBX] -= q * s[bt2];
-    gB[bt2 - kBX] -= q * s[bn];
-  }
-  {
-    const double q = g.F[mt1];
-    gro += q * s[vn] * s[vt1];
-    gv[vn] += q * s[kRO] * s[vt1];
-    gv[vt1] += q * s[kRO] * s[vn];
-    gB[bn - kBX] -= q * s[bt1];
-    gB[bt1 - kBX] -= q * s[bn];
+  if (flux) {
+    // tangential field fluxes
+    {
+      const double q = g.F[bt2];
+      gv[vn] += q * s[bt2];
+      gB[bt2 - kBX] += q * s[vn];
+      gB[bn - kBX] -= q * s[vt2];
+      gv[vt2] -= q * s[bn];
+    }
+    {
+      const double q = g.F[bt1];
+      gv[vn] += q * s[bt1];
+      gB[bt1 - kBX] += q * s[vn];
+      gB[bn - kBX] -= q * s[vt1];
+      gv[vt1] -= q * s[bn];
+    }
+    // energy flux (K vn - vB bn)
+    {
+      const double q = g.F[kEN];
+      const double K = 0.5 * s[kRO] * o.v2 + r2 * s[kPR] + o.B2;
+      const double gK = q * s[vn];
+      gv[vn] += q * K;
+      gvB -= q * s[bn];
+      gB[bn - kBX] -= q * o.vB;
+      gro += 0.5 * o.v2 * gK;
+      gv2 += 0.5 * s[kRO] * gK;
+      gp += r2 * gK;
+      gB2 += gK;
+    }
+    // tangential momentum fluxes
+    {
+      const double q = g.F[mt2];
+      gro += q * s[vn] * s[vt2];
+      gv[vn] += q * s[kRO] * s[vt2];
+      gv[vt2] += q * s[kRO] * s[vn];
+      gB[bn - kBX] -= q * s[bt2];
+      gB[bt2 - kBX] -= q * s[bn];
+    }
+    {
+      const double q = g.F[mt1];
+      gro += q * s[vn] * s[vt1];
+      gv[vn] += q * s[kRO] * s[vt1];
+      gv[vt1] += q * s[kRO] * s[vn];
+      gB[bn - kBX] -= q * s[bt1];
+      gB[bt1 - kBX] -= q * s[bn];
+    }
   }
   // normal momentum flux
   {
@@ -234,10 +247,13 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
   const double SR = (maxR ? R[vn] : L[vn]) + cf;
   double gSL = 0.0, gSR = 0.0;
 
+  bool fxL = false, fxR = false;  // the side's physical flux takes part in the face flux
   if (decide<MODE>(SL >= 0.0, code, tape::kFL)) {
     for (int q = 0; q < 7; ++q) gsL.F[fl[q]] += gF[fl[q]];
+    fxL = true;
   } else if (decide<MODE>(SR <= 0.0, code, tape::kFR)) {
     for (int q = 0; q < 7; ++q) gsR.F[fl[q]] += gF[fl[q]];
+    fxR = true;
   } else {
     const double ih = arcp(SR - SL);
     // HLL state: rho, the normal momentum and Bn here; the tangential
@@ -275,6 +291,9 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
     const bool gbr = decide<MODE>((SL >= (aM - hf * aVL)) || ((aM + hf * aVR) >= SR), code, tape::kG);
     if (gbr) {
       // ---- HLLC-G fallback (flux_solver.f90:450-476) ----
+      side_fwd_tan<DIR>(L, r2, sL);
+      side_fwd_tan<DIR>(R, r2, sR);
+      fxL = fxR = true;
       hll_m(mt1);
       hll_m(mt2);
       hll_p(bt1);
@@ -425,6 +444,7 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
         gUL1bt2 += SL * gF[bt2];
         gL[bt2] -= SL * gF[bt2];
         for (int q = 0; q < 7; ++q) gsL.F[fl[q]] += gF[fl[q]];
+        fxL = true;
       } else if (sRs) {  // F(R*)
         for (int k = 0; k < 3; ++k) {
           gSR += gF[k] * (UR1m[k] - sR.Um[k]);
@@ -442,6 +462,7 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
         gUR1bt2 += SR * gF[bt2];
         gR[bt2] -= SR * gF[bt2];
         for (int q = 0; q < 7; ++q) gsR.F[fl[q]] += gF[fl[q]];
+        fxR = true;
       } else {  // central states
         const double rLs = sqL, rRs = sqR;
         const double ic = arcp(rLs + rRs);
@@ -452,6 +473,8 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
         const double U2bt2 = ic * (rLs * UR1bt2 + rRs * UL1bt2 + rLs * rRs * (vt2R - vt2L) * sg);
         double gat1 = 0, gat2 = 0, gU2bt1 = 0, gU2bt2 = 0, grLs = 0, grRs = 0, gic = 0;
         const bool left = decide<MODE>(aM >= 0.0, code, tape::kSSLeft);
+        fxL = left;
+        fxR = !left;
         const double* S = left ? L : R;
         const Side& sS = left ? sL : sR;
         SideG& gsS = left ? gsL : gsR;
@@ -786,8 +809,8 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
     gsR.a += gamax;
   else
     gsL.a += gamax;
-  side_adj<DIR>(L, gamma, r1, r2, sL, gsL, gL);
-  side_adj<DIR>(R, gamma, r1, r2, sR, gsR, gR);
+  side_adj<DIR>(L, gamma, r1, r2, sL, gsL, gL, fxL);
+  side_adj<DIR>(R, gamma, r1, r2, sR, gsR, gR, fxR);
 }
 
 // Selection code (tape::kLim*) of the minmod (type 1) / MC (type 2)
