@@ -4,6 +4,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 namespace omhd {
 
 struct StepState;
@@ -52,6 +54,22 @@ inline void batch_tile_dims(int kind, int* tx, int* ty) {
   *tx = d[kind & 3][0];
   *ty = d[kind & 3][1];
 }
+// Kernels with more than 48 KB of dynamic shared memory need the attribute
+// set on every device that launches them: once per (kernel, device), tracked
+// in the caller's bit mask (devices 0..63; beyond that, every launch sets it).
+template <class K>
+inline int set_smem_attr_once(K kernel, size_t bytes, std::atomic<unsigned long long>& done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return (int)e;
+  const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ULL << dev) : 0ULL;
+  if (bit && (done.load(std::memory_order_relaxed) & bit)) return 0;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return (int)e;
+  done.fetch_or(bit, std::memory_order_relaxed);
+  return 0;
+}
+
 int launch_stage3d_fp64(const StageArgs& a, cudaStream_t s);
 int launch_stage3d_parity(const StageArgs& a, cudaStream_t s);
 int launch_stage3d_mixed(const StageArgs& a, cudaStream_t s);

@@ -764,18 +764,13 @@ __global__ void __launch_bounds__(NPW * 32 + PipeGeo::NT, 1) k_stage2d_pipe(cons
 template <int FLUX, int TAPE, int NPW = 3>
 int launch_pipe(const StageArgs& a, cudaStream_t s) {
   const size_t bytes = pipe_smem_bytes();
-  static bool configured = false;
-  static int nsm = 0;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_stage2d_pipe<FLUX, TAPE, NPW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)bytes);
-    if (e != cudaSuccess) return (int)e;
-    int dev = 0;
-    e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return (int)e;
-    configured = true;
-  }
+  static std::atomic<unsigned long long> configured{0};
+  int r = set_smem_attr_once(k_stage2d_pipe<FLUX, TAPE, NPW>, bytes, configured);
+  if (r) return r;
+  int dev = 0, nsm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return (int)e;
   const int ntiles = ((a.ix - 2 + PipeGeo::TX - 1) / PipeGeo::TX) * ((a.jx - 2 + PipeGeo::TY - 1) / PipeGeo::TY);
   const int grid = ntiles < nsm ? ntiles : nsm;
   k_stage2d_pipe<FLUX, TAPE, NPW><<<grid, NPW * 32 + PipeGeo::NT, bytes, s>>>(a);
@@ -835,13 +830,9 @@ template <class T, int FLUX, int TAPE = tape::kNone>
 int launch_one(const StageArgs& a, cudaStream_t s) {
   using G = typename GeoFor<T>::type;
   const size_t bytes = G::template smem_bytes<T>();
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e =
-        cudaFuncSetAttribute(k_stage2d<T, FLUX, TAPE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e != cudaSuccess) return (int)e;
-    configured = true;
-  }
+  static std::atomic<unsigned long long> configured{0};
+  const int r = set_smem_attr_once(k_stage2d<T, FLUX, TAPE>, bytes, configured);
+  if (r) return r;
   dim3 grid((a.ix - 2 + G::TX - 1) / G::TX, (a.jx - 2 + G::TY - 1) / G::TY);
   k_stage2d<T, FLUX, TAPE><<<grid, G::NT, bytes, s>>>(a);
   return (int)cudaGetLastError();
@@ -851,13 +842,9 @@ template <class T, int FLUX, class G>
 int launch_batch_one(const StageArgs* args_dev, const int* tile_start_dev, int ngrids, int total_tiles, int ctas,
                      cudaStream_t s) {
   const size_t bytes = G::template smem_bytes<T>();
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e =
-        cudaFuncSetAttribute(k_batch2d<T, FLUX, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e != cudaSuccess) return (int)e;
-    configured = true;
-  }
+  static std::atomic<unsigned long long> configured{0};
+  const int r = set_smem_attr_once(k_batch2d<T, FLUX, G>, bytes, configured);
+  if (r) return r;
   k_batch2d<T, FLUX, G><<<ctas, G::NT, bytes, s>>>(args_dev, tile_start_dev, ngrids, total_tiles);
   return (int)cudaGetLastError();
 }

@@ -434,12 +434,9 @@ __global__ void __launch_bounds__(NT) k_stage3d(const StageArgs a) {
 template <class T, int FLUX>
 int launch_one3d(const StageArgs& a, cudaStream_t s) {
   const size_t bytes = smem3d_bytes<T>();
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_stage3d<T, FLUX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e != cudaSuccess) return (int)e;
-    configured = true;
-  }
+  static std::atomic<unsigned long long> configured{0};
+  const int r = set_smem_attr_once(k_stage3d<T, FLUX>, bytes, configured);
+  if (r) return r;
   dim3 grid((a.ix - 2 + TX - 1) / TX, (a.jx - 2 + TY - 1) / TY, (a.kx - 2 + ZCHUNK - 1) / ZCHUNK);
   k_stage3d<T, FLUX><<<grid, NT, bytes, s>>>(a);
   return (int)cudaGetLastError();
