@@ -144,41 +144,58 @@ __device__ __forceinline__ void phase_load(const StageArgs& a, int bxi, int byi,
   const bool resist = a.eta_kind != OMHD_ETA_NONE;
   const double f1g = a.gamma - 1;  // u2v.f90:11
   T* W = m.W;
-  for (int q = t; q < PL; q += n) {
-    const int rx = q % RX, ry = q / RX;
-    const bool cx_in = rx >= 2 && rx < TX + 2, cy_in = ry >= 2 && ry < TY + 2;
-    if (!cx_in && !cy_in) {
+  // two cells per pass: both cells' loads are issued before either is
+  // converted, so their global-memory latencies overlap
+  constexpr int B = 2;
+  for (int q0 = t; q0 < PL; q0 += B * n) {
+    double u[B][NV];
+    bool act[B];
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      const int q = q0 + b * n;
+      const int rx = q % RX, ry = q / RX;
+      const bool cx_in = rx >= 2 && rx < TX + 2, cy_in = ry >= 2 && ry < TY + 2;
       // corners: only the diagonal neighbours are needed, by the resistive terms
-      if (!resist || rx == 0 || rx == RX - 1 || ry == 0 || ry == RY - 1) continue;
+      act[b] = q < PL && (cx_in || cy_in || (resist && rx != 0 && rx != RX - 1 && ry != 0 && ry != RY - 1));
+      if (act[b]) {
+        const size_t c = (size_t)map_index(gi0 - 2 + rx, ix, perx) + (size_t)ix * map_index(gj0 - 2 + ry, jx, pery);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) u[b][v] = __ldg(a.Uin + v * N + c);
+      }
     }
-    const int gi = gi0 - 2 + rx, gj = gj0 - 2 + ry;
-    const size_t c = (size_t)map_index(gi, ix, perx) + (size_t)ix * map_index(gj, jx, pery);
-    const double* U = a.Uin;
-    const double ro = U[RO * N + c];
-    const double mx = U[MX * N + c], my = U[MY * N + c], mz = U[MZ * N + c];
-    const double iro = rcp_<double, OMHD_FAST>(ro);  // one reciprocal for the three velocities
-    const double vx = divr_<double, OMHD_FAST>(mx, ro, iro), vy = divr_<double, OMHD_FAST>(my, ro, iro),
-                 vz = divr_<double, OMHD_FAST>(mz, ro, iro);  // u2v.f90:24
-    const double rv2 = vx * mx + vy * my + vz * mz;
-    const double bx = U[BX * N + c], by = U[BY * N + c], bz = U[BZ * N + c];
-    const double B2 = bx * bx + by * by + bz * bz;
-    const double pr = f1g * (U[EN * N + c] - 0.5 * (rv2 + B2));  // u2v.f90:27
-    double ps = U[PS * N + c];
-    if (a.stage == 1) ps = glmf * ps;
-    W[VX * PL + q] = T(vx);
-    W[VY * PL + q] = T(vy);
-    W[VZ * PL + q] = T(vz);
-    W[PR * PL + q] = T(pr);
-    W[RO * PL + q] = T(ro);
-    W[BX * PL + q] = T(bx);
-    W[BY * PL + q] = T(by);
-    W[BZ * PL + q] = T(bz);
-    W[PS * PL + q] = T(ps);
-    if (cx_in && cy_in && gi <= ix - 2 && gj <= jx - 2) {  // owner check, u2v.f90:36-45
-      if (pr <= 0)
-        raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, 0, 0, pr);
-      else if (ro <= 0)
-        raise_error(a.err, OMHD_NEG_DENSITY, gi + 1, gj + 1, 0, 0, ro);
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      if (!act[b]) continue;
+      const int q = q0 + b * n;
+      const int rx = q % RX, ry = q / RX;
+      const bool cx_in = rx >= 2 && rx < TX + 2, cy_in = ry >= 2 && ry < TY + 2;
+      const int gi = gi0 - 2 + rx, gj = gj0 - 2 + ry;
+      const double ro = u[b][RO];
+      const double mx = u[b][MX], my = u[b][MY], mz = u[b][MZ];
+      const double iro = rcp_<double, OMHD_FAST>(ro);  // one reciprocal for the three velocities
+      const double vx = divr_<double, OMHD_FAST>(mx, ro, iro), vy = divr_<double, OMHD_FAST>(my, ro, iro),
+                   vz = divr_<double, OMHD_FAST>(mz, ro, iro);  // u2v.f90:24
+      const double rv2 = vx * mx + vy * my + vz * mz;
+      const double bx = u[b][BX], by = u[b][BY], bz = u[b][BZ];
+      const double B2 = bx * bx + by * by + bz * bz;
+      const double pr = f1g * (u[b][EN] - 0.5 * (rv2 + B2));  // u2v.f90:27
+      double ps = u[b][PS];
+      if (a.stage == 1) ps = glmf * ps;
+      W[VX * PL + q] = T(vx);
+      W[VY * PL + q] = T(vy);
+      W[VZ * PL + q] = T(vz);
+      W[PR * PL + q] = T(pr);
+      W[RO * PL + q] = T(ro);
+      W[BX * PL + q] = T(bx);
+      W[BY * PL + q] = T(by);
+      W[BZ * PL + q] = T(bz);
+      W[PS * PL + q] = T(ps);
+      if (cx_in && cy_in && gi <= ix - 2 && gj <= jx - 2) {  // owner check, u2v.f90:36-45
+        if (!gt0_<OMHD_FAST>(pr))
+          raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, 0, 0, pr);
+        else if (!gt0_<OMHD_FAST>(ro))
+          raise_error(a.err, OMHD_NEG_DENSITY, gi + 1, gj + 1, 0, 0, ro);
+      }
     }
   }
 }

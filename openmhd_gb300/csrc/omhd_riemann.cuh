@@ -46,6 +46,14 @@ __device__ __forceinline__ bool lt0_(T x) {  // x < 0
   }
   return x < T(0);
 }
+template <bool FAST>
+__device__ __forceinline__ bool gt0_(double x) {  // x > 0 (false for NaN, as the IEEE compare)
+  if constexpr (FAST) {
+    const long long b = __double_as_longlong(x);
+    return b > 0 && b <= 0x7ff0000000000000LL;
+  }
+  return x > 0.0;
+}
 template <class T, bool FAST>
 __device__ __forceinline__ bool lt_(T a, T b) {  // a < b
   if constexpr (FAST && sizeof(T) == 8) return okey(double(a)) < okey(double(b));
