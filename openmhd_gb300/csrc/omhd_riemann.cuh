@@ -257,10 +257,11 @@ __device__ __forceinline__ void star_state(T ro, T un, T ut1, T ut2, T b1, T b2,
   S[mt2] = ros * v2;
 }
 
-// Per-side quantities of the FP64 HLLD solver (flux_solver.f90:359-401):
-// conserved normal momentum and energy, normal momentum flux, total
-// pressure, v.B and the numerator of the fast speed squared,
-// cf^2 = num / (2 rho).
+// Per-side quantities of the FP64 HLLD solver (flux_solver.f90:359-401)
+// that both sides need: conserved normal momentum, normal momentum flux,
+// total pressure and the numerator of the fast speed squared,
+// cf^2 = num / (2 rho); the conserved energy and v.B (UE, vB) are filled in
+// by hlld_side_e for the sides whose star state or flux is built.
 struct HSide {
   double B2, vB, Umn, UE, Fmn, pt, num;
 };
@@ -270,11 +271,10 @@ __device__ __forceinline__ HSide hlld_side(const double (&S)[NV], double gamma, 
                                            unsigned clamp_bit) {
   constexpr int vn = VX + (DIR - 1) % 3, bn = BX + (DIR - 1) % 3;
   HSide o;
-  const double v2 = S[VX] * S[VX] + S[VY] * S[VY] + S[VZ] * S[VZ];
   o.B2 = S[BX] * S[BX] + S[BY] * S[BY] + S[BZ] * S[BZ];
-  o.vB = S[VX] * S[BX] + S[VY] * S[BY] + S[VZ] * S[BZ];
+  o.vB = 0.0;
+  o.UE = 0.0;
   o.Umn = S[RO] * S[vn];
-  o.UE = 0.5 * (S[RO] * v2 + o.B2) + r1 * S[PR];
   o.pt = S[PR] + 0.5 * o.B2;
   o.Fmn = o.Umn * S[vn] + o.pt - S[bn] * S[bn];  // rho vn^2 + pt - bn^2
   const double f1 = gamma * S[PR], f2 = 4 * (S[bn] * S[bn]);
@@ -282,6 +282,13 @@ __device__ __forceinline__ HSide hlld_side(const double (&S)[NV], double gamma, 
   const bool cl = tape::decide<TAPE>(lt0_<double, true>(D), code, clamp_bit);  // fmax2(D, 0)
   o.num = (f1 + o.B2) + sqrt_nr(cl ? 0.0 : D);
   return o;
+}
+
+// conserved energy and v.B of one side (flux_solver.f90:360-362)
+__device__ __forceinline__ void hlld_side_e(const double (&S)[NV], double r1, HSide& o) {
+  const double v2 = S[VX] * S[VX] + S[VY] * S[VY] + S[VZ] * S[VZ];
+  o.vB = S[VX] * S[BX] + S[VY] * S[BY] + S[VZ] * S[BZ];
+  o.UE = 0.5 * (S[RO] * v2 + o.B2) + r1 * S[PR];
 }
 
 // the physical flux of one side from its primitive state and HSide values
@@ -320,16 +327,18 @@ __device__ __forceinline__ void hlld_f64(const double (&L)[NV], const double (&R
   constexpr int bn = BX + (DIR - 1) % 3, bt1 = BX + DIR % 3, bt2 = BX + (DIR + 1) % 3;
   constexpr int mn = MX + (DIR - 1) % 3, mt1 = MX + DIR % 3, mt2 = MX + (DIR + 1) % 3;
   (void)r2;
-  const HSide hL = hlld_side<DIR, TAPE>(L, gamma, r1, code, tape::kClampL);
-  const HSide hR = hlld_side<DIR, TAPE>(R, gamma, r1, code, tape::kClampR);
+  HSide hL = hlld_side<DIR, TAPE>(L, gamma, r1, code, tape::kClampL);
+  HSide hR = hlld_side<DIR, TAPE>(R, gamma, r1, code, tape::kClampR);
   // largest fast speed: cf^2 = num / (2 rho), numL/rhoL < numR/rhoR <=> numL*rhoR < numR*rhoL
   const bool sr = decide<TAPE>(lt_<double, true>(hL.num * R[RO], hR.num * L[RO]), code, tape::kArSel);
   const double cf = sqrt_ratio_<double, true>(sr ? hR.num : hL.num, 2 * (sr ? R[RO] : L[RO]));
   const double aL = (decide<TAPE>(lt_<double, true>(R[vn], L[vn]), code, tape::kMinR) ? R[vn] : L[vn]) - cf;
   const double aR = (decide<TAPE>(lt_<double, true>(L[vn], R[vn]), code, tape::kMaxR) ? R[vn] : L[vn]) + cf;
   if (decide<TAPE>(ge0_<double, true>(aL), code, tape::kFL)) {
+    hlld_side_e(L, r1, hL);
     hlld_phys_flux<DIR>(L, hL, Fo);
   } else if (decide<TAPE>(le0_<double, true>(aR), code, tape::kFR)) {
+    hlld_side_e(R, r1, hR);
     hlld_phys_flux<DIR>(R, hR, Fo);
   } else {
     // HLL average (:408-417) of rho, the normal momentum and Bn
@@ -352,6 +361,8 @@ __device__ __forceinline__ void hlld_f64(const double (&L)[NV], const double (&R
                      tape::kG)) {
       // HLLC-G fallback :450-476 (rare): the tangential HLL components and
       // both physical fluxes
+      hlld_side_e(L, r1, hL);
+      hlld_side_e(R, r1, hR);
       double FL[NV], FR[NV];
       hlld_phys_flux<DIR>(L, hL, FL);
       hlld_phys_flux<DIR>(R, hR, FR);
@@ -389,11 +400,10 @@ __device__ __forceinline__ void hlld_f64(const double (&L)[NV], const double (&R
       for (int v = 0; v < NV; ++v) Ss[v] = sR ? R[v] : L[v];
       HSide hs;
       hs.B2 = sR ? hR.B2 : hL.B2;
-      hs.vB = sR ? hR.vB : hL.vB;
       hs.Umn = sR ? hR.Umn : hL.Umn;
-      hs.UE = sR ? hR.UE : hL.UE;
       hs.Fmn = sR ? hR.Fmn : hL.Fmn;
       hs.pt = sR ? hR.pt : hL.pt;
+      hlld_side_e(Ss, r1, hs);
       const double as = sR ? aR : aL;
       double S1[NV] = {}, vs1, vs2;
       star_state<double, true, vn, vt1, vt2, bt1, bt2, mn, mt1, mt2>(
@@ -415,11 +425,17 @@ __device__ __forceinline__ void hlld_f64(const double (&L)[NV], const double (&R
         Fo[bt1] = as * (S1[bt1] - Us[bt1]) + Fs[bt1];
         Fo[bt2] = as * (S1[bt2] - Us[bt2]) + Fs[bt2];
       } else {  // central states :533-572, symmetric in (s, o); sigma = +1 for s = L, -1 for s = R
+        double So[NV];  // the other side's primitive state
+#pragma unroll
+        for (int v = 0; v < NV; ++v) So[v] = sR ? L[v] : R[v];
+        HSide ho;
+        ho.B2 = sR ? hL.B2 : hR.B2;
+        ho.pt = sR ? hL.pt : hR.pt;
+        hlld_side_e(So, r1, ho);
         double O1[NV] = {}, vo1, vo2;
         star_state<double, true, vn, vt1, vt2, bt1, bt2, mn, mt1, mt2>(
-            sR ? L[RO] : R[RO], sR ? L[vn] : R[vn], sR ? L[vt1] : R[vt1], sR ? L[vt2] : R[vt2],
-            sR ? L[bt1] : R[bt1], sR ? L[bt2] : R[bt2], sR ? aL : aR, sR ? hL.UE : hR.UE, sR ? hL.pt : hR.pt,
-            sR ? hL.vB : hR.vB, sR ? roL : roR, sR ? ieL : ieR, aM, pt, Ubn, O1, vo1, vo2);
+            So[RO], So[vn], So[vt1], So[vt2], So[bt1], So[bt2], sR ? aL : aR, ho.UE, ho.pt, ho.vB,
+            sR ? roL : roR, sR ? ieL : ieR, aM, pt, Ubn, O1, vo1, vo2);
         const double ros = sR ? roR : roL, roo = sR ? roL : roR;
         const double rss = ros * (sR ? rsR : rsL), rso = roo * (sR ? rsL : rsR);  // sqrt(rho*) of s and o
         const double fc = rcp_nr(rss + rso);
