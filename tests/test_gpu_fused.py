@@ -78,6 +78,31 @@ def test_kelvin_helmholtz_walls_anisotropic(cuda_lib, oracle_mod, precision):
     _cmp(s, g, 1e-12 if precision == "fp64_parity" else 1e-10, "KH")
 
 
+@pytest.mark.parametrize("problem,limiter", [("kh", "minmod"), ("ot", "mc")])
+def test_many_tiles_per_sm_vs_oracle(cuda_lib, oracle_mod, problem, limiter):
+    """Grids with several 16x16 tiles per SM (with ragged edge tiles), so that
+    the persistent FP64 kernel walks tile sequences and reuses both of its
+    face-state buffers: KH 560x300 (walls in y) with minmod and Orszag-Tang
+    416x280 (periodic) with MC, 1 step and 5 steps against the oracle."""
+    from openmhd_gb300 import kelvin_helmholtz, orszag_tang
+
+    if problem == "kh":
+        cfg, model = kelvin_helmholtz(560, 300, precision="fp64")
+    else:
+        cfg, model = orszag_tang(416, 280, precision="fp64", limiter=limiter)
+    assert cfg.limiter == limiter
+    s, g = _pair(cfg, model, oracle_mod)
+    s.step(1)
+    info = s.sync()
+    g.step(1)
+    assert info.status == 0 and abs(info.dt - g.last_dt) <= 1e-14 * g.last_dt
+    _cmp(s, g, 1e-12, "1 step")
+    s.step(4)
+    s.sync()
+    g.step(4)
+    _cmp(s, g, 1e-9, "5 steps")
+
+
 def test_reconnection_walls_resistive_std_rk2(cuda_lib, oracle_mod):
     """2D_reconnection-style walls (sign flips on every side) + resistive fluxes
     (2D_reconnection/flux_resistive.f90) + standard RK2 (rk_std21/22)."""
