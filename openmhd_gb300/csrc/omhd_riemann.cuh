@@ -352,13 +352,19 @@ __device__ __forceinline__ void hlld_f64(const double (&L)[NV], const double (&R
     const double pt = hL.pt + rtL * (aM - L[vn]);
     const double ieL = rcp_nr(aL - aM), ieR = rcp_nr(aR - aM);
     const double roL = rtL * ieL, roR = rtR * ieR;
-    const double rsL = rsqrt_nr(roL), rsR = rsqrt_nr(roR);
     const bool bneg = decide<TAPE>(signbit(Ubn) != 0, code, tape::kBnNeg);
     const double aBn = (TAPE == tape::kNone) ? fabs(Ubn) : (bneg ? -Ubn : Ubn);
-    const double aVL = aBn * rsL, aVR = aBn * rsR;
+    // Alfven speeds aV = |Bn|/sqrt(rho*) enter the HLLC-G switch and the region
+    // only through comparisons, which are made on squares (no square root
+    // unless the central states need sqrt(rho*)):
+    //   aL >= aM - h aV_L  <=>  aM - aL <= 0  or  h^2 Bn^2 >= (aM - aL)^2 rho*_L
+    //   aM + h aV_R >= aR  <=>  aR - aM <= 0  or  h^2 Bn^2 >= (aR - aM)^2 rho*_R
     const double hllg = 1.001;
-    if (decide<TAPE>(!lt_<double, true>(aL, aM - hllg * aVL) || !lt_<double, true>(aM + hllg * aVR, aR), code,
-                     tape::kG)) {
+    const double Bn2 = Ubn * Ubn, hB2 = (hllg * hllg) * Bn2;
+    const double cL = aM - aL, cR = aR - aM;
+    if (decide<TAPE>(le0_<double, true>(cL) || !lt_<double, true>(hB2, (cL * cL) * roL) ||
+                         le0_<double, true>(cR) || !lt_<double, true>(hB2, (cR * cR) * roR),
+                     code, tape::kG)) {
       // HLLC-G fallback :450-476 (rare): the tangential HLL components and
       // both physical fluxes
       hlld_side_e(L, r1, hL);
@@ -390,9 +396,12 @@ __device__ __forceinline__ void hlld_f64(const double (&L)[NV], const double (&R
       Fo[RO] = g1 * (aL * (roL - L[RO]) + FL[RO]) + g2 * (aR * (roR - R[RO]) + FR[RO]);
     } else {
       // region (:482-572), then the side s whose state the flux uses
-      const double aL1 = aM - aVL, aR1 = aM + aVR;
-      const bool sLs = decide<TAPE>(ge0_<double, true>(aL1), code, tape::kLS);
-      const bool sRs = !sLs && decide<TAPE>(le0_<double, true>(aR1), code, tape::kRS);
+      //   aL1 = aM - aV_L >= 0  <=>  aM >= 0 and aM^2 rho*_L >= Bn^2
+      //   aR1 = aM + aV_R <= 0  <=>  aM <= 0 and aM^2 rho*_R >= Bn^2
+      const double aM2 = aM * aM;
+      const bool sLs = decide<TAPE>(ge0_<double, true>(aM) && !lt_<double, true>(aM2 * roL, Bn2), code, tape::kLS);
+      const bool sRs =
+          !sLs && decide<TAPE>(le0_<double, true>(aM) && !lt_<double, true>(aM2 * roR, Bn2), code, tape::kRS);
       const bool cen = !sLs && !sRs;
       const bool sR = sRs || (cen && !decide<TAPE>(ge0_<double, true>(aM), code, tape::kSSLeft));
       double Ss[NV];  // side primitive state
@@ -437,7 +446,8 @@ __device__ __forceinline__ void hlld_f64(const double (&L)[NV], const double (&R
             So[RO], So[vn], So[vt1], So[vt2], So[bt1], So[bt2], sR ? aL : aR, ho.UE, ho.pt, ho.vB,
             sR ? roL : roR, sR ? ieL : ieR, aM, pt, Ubn, O1, vo1, vo2);
         const double ros = sR ? roR : roL, roo = sR ? roL : roR;
-        const double rss = ros * (sR ? rsR : rsL), rso = roo * (sR ? rsL : rsR);  // sqrt(rho*) of s and o
+        const double rsS = rsqrt_nr(ros), rsO = rsqrt_nr(roo);  // 1/sqrt(rho*) of s and o
+        const double rss = ros * rsS, rso = roo * rsO;          // sqrt(rho*) of s and o
         const double fc = rcp_nr(rss + rso);
         const double f2 = (TAPE == tape::kNone) ? fsign(1.0, Ubn) : (bneg ? -1.0 : 1.0);
         const double f2s = sR ? -f2 : f2;
@@ -451,7 +461,7 @@ __device__ __forceinline__ void hlld_f64(const double (&L)[NV], const double (&R
         U2[mn] = ros * aM;
         U2[mt1] = ros * at1;
         U2[mt2] = ros * at2;
-        const double as1 = sR ? aR1 : aL1;
+        const double as1 = sR ? aM + aBn * rsS : aM - aBn * rsS;  // aR1 = aM + aV_R, aL1 = aM - aV_L
 #pragma unroll
         for (int v = MX; v <= EN; ++v) Fo[v] = as1 * U2[v] - (as1 - as) * S1[v] - as * Us[v] + Fs[v];
         Fo[RO] = as1 * U2[RO] - (as1 - as) * S1[RO] - as * Us[RO] + Fs[RO];
