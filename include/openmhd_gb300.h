@@ -251,6 +251,17 @@ int omhd_solver_state_ptr(omhd_solver* s, double** U_dev);
  * put_state applies the boundary conditions and computes the first dt. */
 int omhd_solver_put_state(omhd_solver* s, const double* U, double t);
 int omhd_solver_get_state(omhd_solver* s, double* U);
+/* One call for a driver whose state lives in host memory, the way the
+ * reference's main loop (2D_basic/main.f90:56-188) holds U: put_state(U_in, t)
+ * (U_in == NULL: continue from the state on the device), nsteps steps, and
+ * get_state(U_out), returning the device error code like omhd_solver_sync.
+ * With page-locked host buffers (cudaHostAlloc / cudaHostRegister) the upload
+ * and the first-dt reduction are one pass over the host data, and the last
+ * step writes its result into U_out as it stores it, so no separate copy
+ * follows the steps; other buffers take the put_state / get_state copies.
+ * U_in and U_out may be the same buffer.  Results are those of
+ * put_state + step + get_state, bit for bit. */
+int omhd_solver_step_host(omhd_solver* s, const double* U_in, double* U_out, double t, int nsteps);
 /* fill the state with a model (2D_basic/model.f90 style), apply bc, compute dt */
 int omhd_solver_init_model(omhd_solver* s, const omhd_model* m);
 /* cell-centre coordinates (reference recurrence x(i) = x(i-1) + dx), host arrays */

@@ -101,6 +101,7 @@ SIGNATURES = [
     ("omhd_solver_state_ptr", I, [P, C.POINTER(C.c_void_p)]),
     ("omhd_solver_put_state", I, [P, P, D]),
     ("omhd_solver_get_state", I, [P, P]),
+    ("omhd_solver_step_host", I, [P, P, P, D, I]),
     ("omhd_solver_init_model", I, [P, C.POINTER(Model)]),
     ("omhd_solver_coords", I, [P, P, P, P]),
     ("omhd_solver_set_tend", I, [P, D]),

@@ -35,6 +35,9 @@ struct StageArgs {
   // indexed by the face's lower cell
   unsigned char* tlim;
   unsigned short* tface;
+  // stage 2 of the last step of omhd_solver_step_host: the result is also
+  // written here (the device address of page-locked host memory), else nullptr
+  double* Uhost;
 };
 
 // launchers: return 0 or a CUDA error code

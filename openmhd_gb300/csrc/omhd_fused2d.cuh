@@ -611,7 +611,11 @@ __device__ __forceinline__ double phase_update(const StageArgs& a, int bxi, int 
         const size_t cc = (size_t)xt[q] + (size_t)ix * yt[b];
         const int fm = xf[q] ^ yf[b];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) a.Uout[v * N + cc] = ((fm >> v) & 1) ? -out[v] : out[v];
+        for (int v = 0; v < NV; ++v) {
+          const double o = ((fm >> v) & 1) ? -out[v] : out[v];
+          a.Uout[v * N + cc] = o;
+          if (a.Uhost) a.Uhost[v * N + cc] = o;  // result straight to host memory
+        }
       }
 
     if (a.stage == 2) {  // set_dt.f90:27-37 on the new state

@@ -403,7 +403,11 @@ __global__ void __launch_bounds__(NT) k_stage3d(const StageArgs a) {
             const size_t cc = (size_t)xt[q] + (size_t)ix * ((size_t)yt[b] + (size_t)jx * zt[e]);
             const int fm = xf[q] ^ yf[b] ^ zf[e];
 #pragma unroll
-            for (int v = 0; v < NV; ++v) a.Uout[v * N + cc] = ((fm >> v) & 1) ? -out[v] : out[v];
+            for (int v = 0; v < NV; ++v) {
+              const double o = ((fm >> v) & 1) ? -out[v] : out[v];
+              a.Uout[v * N + cc] = o;
+              if (a.Uhost) a.Uhost[v * N + cc] = o;  // result straight to host memory
+            }
           }
       if (a.stage == 2) {  // 3D_basic/set_dt.f90:27-43 on the new state
         const double ro = out[RO];

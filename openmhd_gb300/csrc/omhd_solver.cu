@@ -197,6 +197,42 @@ __global__ void k_init_cfl(const double* __restrict__ U, int ix, int jx, int kx,
   reduce_and_finalize(st, sc, err, bm, gridDim.x, 0);
 }
 
+// put_state for page-locked host input: one pass copies the state from host
+// memory (through its device address) into U and computes the CFL speed of
+// the interior cells with k_init_cfl's arithmetic, so the upload and the
+// first-dt reduction share one read of the host data
+__global__ void k_upload_cfl(const double* __restrict__ Uh, double* __restrict__ U, int ix, int jx, int kx, int nd,
+                             double gamma, StepState* st, DevError* err, StepConsts sc) {
+  __shared__ double red32[32];
+  const size_t n = (size_t)ix * jx * kx;
+  const double f1g = gamma - 1;
+  double v = 0.0;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    double u[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      u[q] = Uh[q * n + c];
+      U[q * n + c] = u[q];
+    }
+    const int i = (int)(c % ix), j = (int)((c / ix) % jx), k = (int)(c / ((size_t)ix * jx));
+    const bool interior = i >= 1 && i <= ix - 2 && j >= 1 && j <= jx - 2 && (nd != 3 || (k >= 1 && k <= kx - 2));
+    if (!interior) continue;
+    const double ro = u[RO];
+    const double mx = u[MX], my = u[MY], mz = u[MZ];
+    const double vx = mx / ro, vy = my / ro, vz = mz / ro;
+    const double rv2 = vx * mx + vy * my + vz * mz;
+    const double bx = u[BX], by = u[BY], bz = u[BZ];
+    const double B2 = bx * bx + by * by + bz * bz;
+    const double pr = f1g * (u[EN] - 0.5 * (rv2 + B2));
+    const double f1 = gamma * pr;
+    double sp = fmax2(fabs(vx) + fast_speed(f1, B2, bx, ro), fabs(vy) + fast_speed(f1, B2, by, ro));
+    if (nd == 3) sp = fmax2(sp, fabs(vz) + fast_speed(f1, B2, bz, ro));
+    v = fmax2(sp, v);
+  }
+  const double bm = block_max_pos(v, red32);
+  reduce_and_finalize(st, sc, err, bm, gridDim.x, 0);
+}
+
 __global__ void k_set_tend(StepState* st, double tend) {
   st->tend = tend;
   st->done = (st->t >= tend) ? 1 : 0;
@@ -312,7 +348,8 @@ int apply_bc(omhd_solver* s) {
   return cerr(s, cudaGetLastError(), "bc kernel");
 }
 
-int plan_first(omhd_solver* s, double t) {
+// new run from time t: step record and error word reset on the stream
+int reset_run(omhd_solver* s, double t) {
   const omhd_config& c = s->cfg;
   StepState h;
   memset(&h, 0, sizeof h);
@@ -324,6 +361,13 @@ int plan_first(omhd_solver* s, double t) {
   if (r) return r;
   s->last_status = OMHD_OK;
   memset(&s->last, 0, sizeof s->last);
+  return OMHD_OK;
+}
+
+int plan_first(omhd_solver* s, double t) {
+  const omhd_config& c = s->cfg;
+  int r = reset_run(s, t);
+  if (r) return r;
   const long long cells = (long long)(c.ix - 2) * (c.jx - 2) * (c.nd == 3 ? c.kx - 2 : 1);
   int blocks = ceil_div(cells, TPB);
   if (blocks > 152 * 8) blocks = 152 * 8;
@@ -499,6 +543,80 @@ int omhd_solver_step(omhd_solver* s, int nsteps) {
     if (r) return r;
   }
   return OMHD_OK;
+}
+
+// device address of page-locked (or registered) host memory, else nullptr
+static double* mapped_host(const void* p) {
+  cudaPointerAttributes at;
+  if (!p || cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+  return static_cast<double*>(at.devicePointer);
+}
+
+int omhd_solver_step_host(omhd_solver* s, const double* U_in, double* U_out, double t, int nsteps) {
+  if (!s || !U_out || nsteps < 1) return OMHD_BAD_ARG;
+  int r = ensure_state(s);
+  if (r) return r;
+  const omhd_config& c = s->cfg;
+  const size_t n = (size_t)c.ix * c.jx * c.kx;
+  // input: one fused upload + first-dt pass from page-locked memory, else put_state
+  if (U_in) {
+    const double* din = mapped_host(U_in);
+    if (din) {
+      r = reset_run(s, t);
+      if (r) return r;
+      int blocks = ceil_div((long long)n, TPB);
+      if (blocks > 152 * 8) blocks = 152 * 8;
+      k_upload_cfl<<<blocks, TPB, 0, s->stream>>>(din, s->U, c.ix, c.jx, c.kx, c.nd, c.gamma, s->st, s->err,
+                                                  consts_of(s));
+      r = cerr(s, cudaGetLastError(), "upload kernel");
+      if (!r) r = apply_bc(s);
+    } else {
+      r = omhd_solver_put_state(s, U_in, t);
+    }
+    if (r) return r;
+  }
+  StepState before;
+  r = cerr(s, cudaMemcpyAsync(&before, s->st, sizeof before, cudaMemcpyDeviceToHost, s->stream), "step record read");
+  if (!r) r = cerr(s, cudaStreamSynchronize(s->stream), "step record sync");
+  if (r) return r;
+  // output: the last stage 2 writes the result into page-locked memory as it
+  // stores it, else (or if that stage did not run) a copy after the steps
+  double* dout = mapped_host(U_out);
+  for (int k = 0; k < nsteps; ++k) {
+    r = launch_stage(s, 1);
+    if (r) return r;
+    if (k == nsteps - 1 && dout) {
+      StageArgs a = make_stage_args(s, 2);
+      a.Uhost = dout;
+      int e;
+      if (c.nd == 2)
+        e = (c.precision == OMHD_PREC_FP64)          ? launch_stage2d_fp64(a, s->stream)
+            : (c.precision == OMHD_PREC_FP64_PARITY) ? launch_stage2d_parity(a, s->stream)
+                                                     : launch_stage2d_mixed(a, s->stream);
+      else
+        e = (c.precision == OMHD_PREC_FP64)          ? launch_stage3d_fp64(a, s->stream)
+            : (c.precision == OMHD_PREC_FP64_PARITY) ? launch_stage3d_parity(a, s->stream)
+                                                     : launch_stage3d_mixed(a, s->stream);
+      r = cerr(s, (cudaError_t)e, "stage kernel launch");
+    } else {
+      r = launch_stage(s, 2);
+    }
+    if (r) return r;
+  }
+  StepState after;
+  r = cerr(s, cudaMemcpyAsync(&after, s->st, sizeof after, cudaMemcpyDeviceToHost, s->stream), "step record read");
+  if (!r) r = cerr(s, cudaStreamSynchronize(s->stream), "step record sync");
+  if (r) return r;
+  if (!dout || after.steps != before.steps + nsteps) {
+    r = cerr(s, cudaMemcpyAsync(U_out, s->U, sizeof(double) * NV * n, cudaMemcpyDefault, s->stream), "state download");
+    if (!r) r = cerr(s, cudaStreamSynchronize(s->stream), "state download sync");
+    if (r) return r;
+  }
+  return omhd_solver_sync(s, nullptr);
 }
 
 int omhd_solver_step_graph(omhd_solver* s, int nsteps, int replays) {

@@ -15,7 +15,10 @@ from dataclasses import dataclass, field
 
 from . import _lib
 
-OMHD_TIMEOUT = 5  # omhd_status_t
+OMHD_BAD_ARG = 4  # omhd_status_t
+OMHD_TIMEOUT = 5
+OMHD_CUDA_ERR = 6
+OMHD_NOT_SUPPORTED = 7
 LIMITERS = {"flat": 0, "minmod": 1, "mc": 2, "vanleer": 3, "koren": 4}
 FLUXES = {"llf": 0, "hll": 1, "hllc": 2, "hlld": 3, "lhlld": 4}
 PRECISIONS = {"fp64": 0, "fp64_parity": 1, "mixed": 2}
@@ -257,6 +260,40 @@ class Solver:
             self._check(self.lib.omhd_solver_put_state(self._h, src.data_ptr(), float(t)))
             self.sync()
         return self
+
+    def step_host(self, U_in, U_out=None, t: float = 0.0, n: int = 1) -> int:
+        """Host state in, `n` steps, host state out, in one call
+        (omhd_solver_step_host): U_in / U_out are CPU torch tensors or numpy
+        arrays of the state's shape (float64, contiguous); U_in None continues
+        from the device state, U_out None writes back into U_in.  Page-locked
+        tensors (pin_memory) take the fused upload and the direct write of the
+        result.  Returns the device error code (0: no error)."""
+        import torch
+
+        def ptr(a):
+            if a is None:
+                return None
+            if isinstance(a, torch.Tensor):
+                if a.device.type != "cpu" or a.dtype != torch.float64 or not a.is_contiguous():
+                    raise ValueError("step_host takes contiguous float64 CPU tensors")
+                return a.data_ptr()
+            if a.dtype.str != "<f8" or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError("step_host takes contiguous float64 arrays")
+            return a.ctypes.data
+
+        if U_out is None:
+            U_out = U_in
+        if U_out is None:
+            raise ValueError("step_host needs an output buffer")
+        for a in (U_in, U_out):
+            if a is not None and tuple(a.shape) != tuple(self.cfg.shape):
+                raise ValueError(f"state shape {tuple(a.shape)} != {tuple(self.cfg.shape)}")
+        self.stream.wait_stream(torch.cuda.current_stream())
+        st = self.lib.omhd_solver_step_host(self._h, ptr(U_in), ptr(U_out), float(t), int(n))
+        if st in (OMHD_BAD_ARG, OMHD_CUDA_ERR):
+            self._check(st)
+        torch.cuda.current_stream().wait_stream(self.stream)
+        return st
 
     def state(self):
         """The bound state tensor (valid after sync())."""
