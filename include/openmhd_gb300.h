@@ -295,7 +295,10 @@ int omhd_ensemble_member(omhd_ensemble* e, int i, omhd_solver** s);
 int omhd_ensemble_init_models(omhd_ensemble* e, const omhd_model* models);
 /* tile_kind 0: 32x8, 1: 32x4, 2: 16x16, 3: 64x4 cells per CTA; CTAs = ctas_per_sm x SMs */
 int omhd_ensemble_set_tiling(omhd_ensemble* e, int tile_kind, int ctas_per_sm);
-/* time `steps` real steps per candidate tiling and keep the fastest */
+/* time `steps` real steps per candidate tiling, each from the same ensemble
+ * state (saved and restored: tuning leaves the states, times and step counts
+ * unchanged; it allocates a copy of the ensemble's state pool meanwhile), and
+ * keep the fastest */
 int omhd_ensemble_autotune(omhd_ensemble* e, int steps, int* tile_kind, int* ctas_per_sm, double* ms_per_step);
 int omhd_ensemble_step(omhd_ensemble* e, int nsteps);
 int omhd_ensemble_step_graph(omhd_ensemble* e, int nsteps, int replays);

@@ -121,7 +121,7 @@ int omhd_ensemble_create(const omhd_config* cfgs, int n, omhd_ensemble** out) {
   }
   if (!r) r = ecuda(cudaMalloc(&e->args_dev[0], sizeof(StageArgs) * n));
   if (!r) r = ecuda(cudaMalloc(&e->args_dev[1], sizeof(StageArgs) * n));
-  if (!r) r = ecuda(cudaMalloc(&e->tile_start_dev, sizeof(int) * (n + 1)));
+  if (!r) r = ecuda(cudaMalloc(&e->tile_start_dev, sizeof(int) * (n + 2)));  // prefix sums + work counter
   if (!r) r = upload_args(e);
   if (!r) r = build_tiles(e);
   if (r) {
@@ -202,6 +202,34 @@ int omhd_ensemble_step_graph(omhd_ensemble* e, int nsteps, int replays) {
 // tuning are ordinary steps of the run) and keeps the fastest.
 int omhd_ensemble_autotune(omhd_ensemble* e, int steps, int* best_kind, int* best_ctas, double* best_ms) {
   if (!e || steps <= 0) return OMHD_BAD_ARG;
+  // every candidate is timed from the same ensemble state: the states, step
+  // records and error words are saved here and put back before each
+  // measurement and at the end, so tuning leaves the ensemble where it was
+  size_t pool_doubles = 0;
+  for (int i = 0; i < e->n; ++i) pool_doubles += 2 * e->members[i]->n * NV;
+  double* snap = nullptr;
+  std::vector<StepState> st_h(e->n);
+  std::vector<DevError> er_h(e->n);
+  if (cudaStreamSynchronize(e->stream) != cudaSuccess) return OMHD_CUDA_ERR;
+  if (cudaMalloc(&snap, sizeof(double) * pool_doubles) != cudaSuccess) return OMHD_CUDA_ERR;
+  int rs = ecuda(cudaMemcpy(snap, e->pool, sizeof(double) * pool_doubles, cudaMemcpyDeviceToDevice));
+  for (int i = 0; i < e->n && !rs; ++i) {
+    rs = ecuda(cudaMemcpy(&st_h[i], e->members[i]->st, sizeof(StepState), cudaMemcpyDeviceToHost));
+    if (!rs) rs = ecuda(cudaMemcpy(&er_h[i], e->members[i]->err, sizeof(DevError), cudaMemcpyDeviceToHost));
+  }
+  auto restore = [&]() -> int {
+    if (cudaStreamSynchronize(e->stream) != cudaSuccess) return OMHD_CUDA_ERR;
+    int r = ecuda(cudaMemcpy(e->pool, snap, sizeof(double) * pool_doubles, cudaMemcpyDeviceToDevice));
+    for (int i = 0; i < e->n && !r; ++i) {
+      r = ecuda(cudaMemcpy(e->members[i]->st, &st_h[i], sizeof(StepState), cudaMemcpyHostToDevice));
+      if (!r) r = ecuda(cudaMemcpy(e->members[i]->err, &er_h[i], sizeof(DevError), cudaMemcpyHostToDevice));
+    }
+    return r;
+  };
+  if (rs) {
+    cudaFree(snap);
+    return rs;
+  }
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
@@ -213,6 +241,7 @@ int omhd_ensemble_autotune(omhd_ensemble* e, int steps, int* best_kind, int* bes
       if (r) continue;
       r = omhd_ensemble_step(e, 1);  // warm-up: first launch configures the kernel
       if (r) continue;
+      if (restore()) break;
       cudaEventRecord(a, e->stream);
       r = omhd_ensemble_step(e, steps);
       cudaEventRecord(b, e->stream);
@@ -228,6 +257,9 @@ int omhd_ensemble_autotune(omhd_ensemble* e, int steps, int* best_kind, int* bes
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   cudaGetLastError();
+  const int rr = restore();
+  cudaFree(snap);
+  if (rr) return rr;
   if (best_kind) *best_kind = bk;
   if (best_ctas) *best_ctas = bc;
   if (best_ms) *best_ms = best;

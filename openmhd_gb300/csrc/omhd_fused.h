@@ -47,9 +47,9 @@ int launch_stage2d_mixed(const StageArgs& a, cudaStream_t s);
 // fp64 HLLD stage with a decision tape: mode tape::kRecord or tape::kReplay
 int launch_stage2d_fp64_tape(const StageArgs& a, int mode, cudaStream_t s);
 // ensemble launchers: tile_kind 0: 32x8, 1: 32x4, 2: 16x16, 3: 64x4 cells per CTA
-int launch_batch2d_fp64(int flux, int tile_kind, const StageArgs* args_dev, const int* tile_start_dev, int ngrids,
+int launch_batch2d_fp64(int flux, int tile_kind, const StageArgs* args_dev, int* tile_start_dev, int ngrids,
                         int total_tiles, int ctas, cudaStream_t s);
-int launch_batch2d_mixed(int flux, int tile_kind, const StageArgs* args_dev, const int* tile_start_dev, int ngrids,
+int launch_batch2d_mixed(int flux, int tile_kind, const StageArgs* args_dev, int* tile_start_dev, int ngrids,
                          int total_tiles, int ctas, cudaStream_t s);
 constexpr int kBatchTileKinds = 4;
 inline void batch_tile_dims(int kind, int* tx, int* ty) {

@@ -798,19 +798,25 @@ int launch_pipe(const StageArgs& a, cudaStream_t s) {
   return (int)cudaGetLastError();
 }
 
-// Ensemble of independent 2D grids in one persistent launch: CTAs loop over
-// the tiles of all grids (work item w -> grid by binary search of the tile
-// prefix sums), each grid keeps its own dt, step record and error word, and
-// the CTA that finishes the last tile of a grid in stage 2 plans that grid's
-// next step.
+// Ensemble of independent 2D grids in one persistent launch: CTAs take the
+// tiles of all grids from a work counter (*queue, zero at launch; work item
+// w -> grid by binary search of the tile prefix sums), so members that are
+// cheap this step (finished, or failed) leave no CTA idle; each grid keeps its
+// own dt, step record and error word, and the CTA that finishes the last tile
+// of a grid in stage 2 plans that grid's next step.
 template <class T, int FLUX, class G>
 __global__ void __launch_bounds__(G::NT) k_batch2d(const StageArgs* __restrict__ args,
-                                                   const int* __restrict__ tile_start, int ngrids, int total_tiles) {
+                                                   const int* __restrict__ tile_start, int ngrids, int total_tiles,
+                                                   int* __restrict__ queue) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red32[32];
   __shared__ unsigned int is_last;
-  __shared__ int skip_s;
-  for (int w = blockIdx.x; w < total_tiles; w += gridDim.x) {
+  __shared__ int skip_s, w_s;
+  for (;;) {
+    if (threadIdx.x == 0) w_s = atomicAdd(queue, 1);
+    __syncthreads();
+    const int w = w_s;  // uniform; rewritten only after the barrier that ends this item
+    if (w >= total_tiles) break;
     int lo = 0, hi = ngrids - 1;  // last grid with tile_start <= w
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
@@ -860,20 +866,23 @@ int launch_one(const StageArgs& a, cudaStream_t s) {
 }
 
 template <class T, int FLUX, class G>
-int launch_batch_one(const StageArgs* args_dev, const int* tile_start_dev, int ngrids, int total_tiles, int ctas,
+int launch_batch_one(const StageArgs* args_dev, int* tile_start_dev, int ngrids, int total_tiles, int ctas,
                      cudaStream_t s) {
   const size_t bytes = G::template smem_bytes<T>();
   static std::atomic<unsigned long long> configured{0};
   const int r = set_smem_attr_once(k_batch2d<T, FLUX, G>, bytes, configured);
   if (r) return r;
-  k_batch2d<T, FLUX, G><<<ctas, G::NT, bytes, s>>>(args_dev, tile_start_dev, ngrids, total_tiles);
+  int* queue = tile_start_dev + ngrids + 1;  // work counter after the prefix sums
+  cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(int), s);
+  if (e != cudaSuccess) return (int)e;
+  k_batch2d<T, FLUX, G><<<ctas, G::NT, bytes, s>>>(args_dev, tile_start_dev, ngrids, total_tiles, queue);
   return (int)cudaGetLastError();
 }
 
 // Batched launch with one of the tile shapes the ensemble autotuner chooses
 // from (HLLD only: the ensemble configuration's Riemann solver).
 template <class T>
-int launch_batch_variant(int flux, int tile_kind, const StageArgs* args, const int* tile_start, int ngrids,
+int launch_batch_variant(int flux, int tile_kind, const StageArgs* args, int* tile_start, int ngrids,
                          int total_tiles, int ctas, cudaStream_t s) {
   if (flux != FX_HLLD) return (int)cudaErrorNotSupported;
   switch (tile_kind) {

@@ -31,7 +31,7 @@ int launch_stage2d_fp64_tape(const StageArgs& a, int mode, cudaStream_t s) {
 }  // namespace omhd
 
 namespace omhd {
-int launch_batch2d_fp64(int flux, int tile_kind, const StageArgs* args_dev, const int* tile_start_dev, int ngrids,
+int launch_batch2d_fp64(int flux, int tile_kind, const StageArgs* args_dev, int* tile_start_dev, int ngrids,
                       int total_tiles, int ctas, cudaStream_t s) {
   return v_fp64::launch_batch_variant<double>(flux, tile_kind, args_dev, tile_start_dev, ngrids, total_tiles, ctas, s);
 }

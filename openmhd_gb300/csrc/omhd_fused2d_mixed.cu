@@ -9,7 +9,7 @@ int launch_stage2d_mixed(const StageArgs& a, cudaStream_t s) { return v_mixed::l
 }  // namespace omhd
 
 namespace omhd {
-int launch_batch2d_mixed(int flux, int tile_kind, const StageArgs* args_dev, const int* tile_start_dev, int ngrids,
+int launch_batch2d_mixed(int flux, int tile_kind, const StageArgs* args_dev, int* tile_start_dev, int ngrids,
                       int total_tiles, int ctas, cudaStream_t s) {
   return v_mixed::launch_batch_variant<float>(flux, tile_kind, args_dev, tile_start_dev, ngrids, total_tiles, ctas, s);
 }

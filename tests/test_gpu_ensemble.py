@@ -25,7 +25,7 @@ def test_members_match_single_grid_runs(cuda_lib, precision, tol):
     infos = ens.sync()
     for i, (c, m) in enumerate(zip(cfgs, models)):
         s = Solver(c).init_model(m)
-        s.step(3 + 8 + 8)  # autotune ran 8 candidates x (1 warm-up + 1 timed) steps
+        s.step(3)  # the autotuner leaves the ensemble state where it found it
         ref = s.get_state_numpy()
         info = s.sync()
         assert infos[i].steps == info.steps
@@ -48,3 +48,20 @@ def test_graph_replay_and_per_member_dt(cuda_lib):
     for i in range(len(cfgs)):
         assert ia[i].steps == ib[i].steps == 6
         assert np.array_equal(a.member_state(i), b.member_state(i))
+
+
+def test_autotune_leaves_state_unchanged(cuda_lib):
+    """Every candidate tiling is timed from the same saved state, and the
+    state, times and step counts are put back afterwards, bit for bit."""
+    from openmhd_gb300.ensemble import Ensemble, batched_problem_set
+
+    cfgs, models = batched_problem_set(5, seed=7, precision="mixed", sides=[48, 80])
+    ens = Ensemble(cfgs).init_models(models)
+    ens.step(2)
+    before = [ens.member_state(i).copy() for i in range(len(cfgs))]
+    info0 = ens.sync()
+    ens.autotune(steps=2)
+    info1 = ens.sync()
+    for i in range(len(cfgs)):
+        assert np.array_equal(ens.member_state(i), before[i])
+        assert info1[i].steps == info0[i].steps and info1[i].t == info0[i].t
