@@ -82,8 +82,8 @@ OMHD_HD void side_fwd(const double* s, double gamma, double r1, double r2, Side&
   const double Dc = decide<MODE>(0.0 > o.D, code, clamp_bit) ? 0.0 : o.D;  // fmax2(D, 0)
   o.isq = (Dc > 0.0) ? arsqrt(Dc) : 0.0;
   o.sq = Dc * o.isq;
-  o.ir = arcp(s[kRO]);
-  o.a = (o.Q + o.sq) * (0.5 * o.ir);
+  o.ir = 0.0;  // 1/rho and the fast speed squared a = (Q + sq)/(2 rho): set by
+  o.a = 0.0;   // hlld_vjp for the side whose speed is the larger (side_cf)
   o.pt = s[kPR] + 0.5 * o.B2;
 }
 
@@ -101,11 +101,19 @@ OMHD_HD void side_fwd_tan(const double* s, double r2, Side& o) {
   o.F[bt2] = s[vn] * s[bt2] - s[bn] * s[vt2];
 }
 
+// 1/rho and the fast speed squared a = (Q + sq)/(2 rho) of one side
+OMHD_HD void side_cf(const double* s, Side& o) {
+  o.ir = arcp(s[kRO]);
+  o.a = (o.Q + o.sq) * (0.5 * o.ir);
+}
+
 // flux = false: the side's tangential momentum, energy and tangential field
-// fluxes carry no gradient (g.F is zero there), and their reverse is skipped
+// fluxes carry no gradient (g.F is zero there), and their reverse is skipped;
+// cf = false: the side's fast speed is not the face's (g.a is zero), and the
+// reverse of its fast-speed chain is skipped
 template <int DIR>
 OMHD_HD void side_adj(const double* s, double gamma, double r1, double r2, const Side& o, const SideG& g,
-                      double* gs, bool flux = true) {
+                      double* gs, bool flux = true, bool cf = true) {
   constexpr int vn = (DIR - 1) % 3, vt1 = DIR % 3, vt2 = (DIR + 1) % 3;
   constexpr int bn = kBX + (DIR - 1) % 3, bt1 = kBX + DIR % 3, bt2 = kBX + (DIR + 1) % 3;
   constexpr int mn = vn, mt1 = vt1, mt2 = vt2;
@@ -114,19 +122,21 @@ OMHD_HD void side_adj(const double* s, double gamma, double r1, double r2, const
   // pt = p + B2/2
   gp += g.pt;
   gB2 += 0.5 * g.pt;
-  // a = (Q + sq) / (2 rho)
-  const double gnum = g.a * (0.5 * o.ir);
-  gro -= g.a * o.a * o.ir;
-  double gQ = gnum;
-  const double gsq = gnum;
-  const double gD = (o.D > 0.0) ? gsq * 0.5 * o.isq : 0.0;
-  gQ += 2 * o.Q * gD;
-  double gf1 = -o.f2 * gD;
-  const double gf2 = -o.f1 * gD;
-  gf1 += gQ;
-  gB2 += gQ;
-  gB[bn - kBX] += 8 * s[bn] * gf2;
-  gp += gamma * gf1;
+  if (cf) {
+    // a = (Q + sq) / (2 rho)
+    const double gnum = g.a * (0.5 * o.ir);
+    gro -= g.a * o.a * o.ir;
+    double gQ = gnum;
+    const double gsq = gnum;
+    const double gD = (o.D > 0.0) ? gsq * 0.5 * o.isq : 0.0;
+    gQ += 2 * o.Q * gD;
+    double gf1 = -o.f2 * gD;
+    const double gf2 = -o.f1 * gD;
+    gf1 += gQ;
+    gB2 += gQ;
+    gB[bn - kBX] += 8 * s[bn] * gf2;
+    gp += gamma * gf1;
+  }
   if (flux) {
     // tangential field fluxes
     {
@@ -237,7 +247,12 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
   zero(gsR);
   const int fl[7] = {kRO, mn, mt1, mt2, kEN, bt1, bt2};  // slots set from the physical fluxes
 
-  const bool aRsel = decide<MODE>(sR.a > sL.a, code, tape::kArSel);  // fmax2(aL, aR)
+  // fmax2(aL, aR) of a = (Q + sq)/(2 rho): aL < aR <=> (Q + sq)_L rho_R < (Q + sq)_R rho_L
+  const bool aRsel = decide<MODE>((sL.Q + sL.sq) * R[kRO] < (sR.Q + sR.sq) * L[kRO], code, tape::kArSel);
+  if (aRsel)
+    side_cf(R, sR);
+  else
+    side_cf(L, sL);
   const double amax = aRsel ? sR.a : sL.a;
   const double icf = (amax > 0.0) ? arsqrt(amax) : 0.0;
   const double cf = amax * icf;
@@ -809,8 +824,8 @@ OMHD_HD void hlld_vjp(const double* L, const double* R, double ch, double gamma,
     gsR.a += gamax;
   else
     gsL.a += gamax;
-  side_adj<DIR>(L, gamma, r1, r2, sL, gsL, gL, fxL);
-  side_adj<DIR>(R, gamma, r1, r2, sR, gsR, gR, fxR);
+  side_adj<DIR>(L, gamma, r1, r2, sL, gsL, gL, fxL, !aRsel);
+  side_adj<DIR>(R, gamma, r1, r2, sR, gsR, gR, fxR, aRsel);
 }
 
 // Selection code (tape::kLim*) of the minmod (type 1) / MC (type 2)
