@@ -144,9 +144,10 @@ __device__ __forceinline__ void phase_load(const StageArgs& a, int bxi, int byi,
   const bool resist = a.eta_kind != OMHD_ETA_NONE;
   const double f1g = a.gamma - 1;  // u2v.f90:11
   T* W = m.W;
-  // two cells per pass: both cells' loads are issued before either is
-  // converted, so their global-memory latencies overlap
-  constexpr int B = 2;
+  // FP64: two cells per pass, both cells' loads issued before either is
+  // converted, so their global-memory latencies overlap; FP32-mixed (two CTAs
+  // per SM, 112 registers) one cell per pass
+  constexpr int B = sizeof(T) == 8 ? 2 : 1;
   for (int q0 = t; q0 < PL; q0 += B * n) {
     double u[B][NV];
     bool act[B];
@@ -568,12 +569,23 @@ __device__ __forceinline__ double phase_update(const StageArgs& a, int bxi, int 
   const bool perx = a.bc_kind[0] == OMHD_BC_PERIODIC, pery = a.bc_kind[2] == OMHD_BC_PERIODIC;
   const double gamma = a.gamma;
   const double f1g = gamma - 1;
+  // the argument block may live in global memory (ensembles), where a store to
+  // the state could alias it: every pointer and scalar used in the loop is
+  // read once, here
+  double* const Uout = a.Uout;
+  double* const Uhost = a.Uhost;
+  const double* const Ubase = a.Ubase;
+  const double* const U1 = a.U1;
+  const double dtx = a.dtx_scale * dt / a.dx, dty = a.dtx_scale * dt / a.dy;
+  const bool iso = a.iso, rk2 = a.stage == 1 || a.time_type == OMHD_TIME_RK2, stage2 = a.stage == 2;
+  int flip[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) flip[q] = a.bc_flip[q];
   double vcell = 0.0;
   for (int k = t; k < TX * TY; k += n) {
     const int tx = k % TX, ty = k / TX;
     const int gi = gi0 + tx, gj = gj0 + ty;
     if (gi > ix - 2 || gj > jx - 2) continue;
-    const double dtx = a.dtx_scale * dt / a.dx, dty = a.dtx_scale * dt / a.dy;
     const size_t c = (size_t)gi + (size_t)ix * gj;
     double out[NV];
 #pragma unroll
@@ -583,18 +595,18 @@ __device__ __forceinline__ double phase_update(const StageArgs& a, int bxi, int 
       const double dF = fx[0] - fx[1];
       const double gm = m.FY[v * m.fyv + ty * TX + tx], gp = m.FY[v * m.fyv + (ty + 1) * TX + tx];
       double d;
-      if (a.iso)
+      if (iso)
         d = dtx * (dF + gm - gp);  // rk.f90:26-35 operation order
       else
         d = dtx * dF + dty * (gm - gp);
-      double ub = a.Ubase[v * N + c];
+      double ub = Ubase[v * N + c];
       if (v == PS) ub = glmf * ub;
-      if (a.stage == 1 || a.time_type == OMHD_TIME_RK2)
+      if (rk2)
         out[v] = ub + d;  // rk_tvd21 / rk_std21 / rk_std22
       else
-        out[v] = 0.5 * (ub + a.U1[v * N + c] + d);  // rk_tvd22 (rk.f90:56-66)
+        out[v] = 0.5 * (ub + U1[v * N + c] + d);  // rk_tvd22 (rk.f90:56-66)
     }
-    if (a.stage == 2) out[PS] = glmf * out[PS];  // second GLM half (main.f90:185)
+    if (stage2) out[PS] = glmf * out[PS];  // second GLM half (main.f90:185)
 
     // owner-writes ghost fill (bc.f90 order: x sides, then y sides)
     int xt[3], yt[3], xf[3], yf[3], nxt = 1, nyt = 1;
@@ -602,10 +614,10 @@ __device__ __forceinline__ double phase_update(const StageArgs& a, int bxi, int 
     xf[0] = 0;
     yt[0] = gj;
     yf[0] = 0;
-    if (gi == 1) { xt[nxt] = perx ? ix - 1 : 0; xf[nxt] = perx ? 0 : a.bc_flip[0]; ++nxt; }
-    if (gi == ix - 2) { xt[nxt] = perx ? 0 : ix - 1; xf[nxt] = perx ? 0 : a.bc_flip[1]; ++nxt; }
-    if (gj == 1) { yt[nyt] = pery ? jx - 1 : 0; yf[nyt] = pery ? 0 : a.bc_flip[2]; ++nyt; }
-    if (gj == jx - 2) { yt[nyt] = pery ? 0 : jx - 1; yf[nyt] = pery ? 0 : a.bc_flip[3]; ++nyt; }
+    if (gi == 1) { xt[nxt] = perx ? ix - 1 : 0; xf[nxt] = perx ? 0 : flip[0]; ++nxt; }
+    if (gi == ix - 2) { xt[nxt] = perx ? 0 : ix - 1; xf[nxt] = perx ? 0 : flip[1]; ++nxt; }
+    if (gj == 1) { yt[nyt] = pery ? jx - 1 : 0; yf[nyt] = pery ? 0 : flip[2]; ++nyt; }
+    if (gj == jx - 2) { yt[nyt] = pery ? 0 : jx - 1; yf[nyt] = pery ? 0 : flip[3]; ++nyt; }
     for (int b = 0; b < nyt; ++b)
       for (int q = 0; q < nxt; ++q) {
         const size_t cc = (size_t)xt[q] + (size_t)ix * yt[b];
@@ -613,12 +625,12 @@ __device__ __forceinline__ double phase_update(const StageArgs& a, int bxi, int 
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
           const double o = ((fm >> v) & 1) ? -out[v] : out[v];
-          a.Uout[v * N + cc] = o;
-          if (a.Uhost) a.Uhost[v * N + cc] = o;  // result straight to host memory
+          Uout[v * N + cc] = o;
+          if (Uhost) Uhost[v * N + cc] = o;  // result straight to host memory
         }
       }
 
-    if (a.stage == 2) {  // set_dt.f90:27-37 on the new state
+    if (stage2) {  // set_dt.f90:27-37 on the new state
       const double ro = out[RO];
       const double iro = rcp_<double, OMHD_FAST>(ro);  // one reciprocal for the three velocities
       const double vx = divr_<double, OMHD_FAST>(out[MX], ro, iro), vy = divr_<double, OMHD_FAST>(out[MY], ro, iro),
@@ -660,7 +672,7 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
 
 // one CTA per tile of one grid
 template <class T, int FLUX, int TAPE = tape::kNone>
-__global__ void __launch_bounds__(GeoFor<T>::type::NT) k_stage2d(const StageArgs a) {
+__global__ void __launch_bounds__(GeoFor<T>::type::NT, sizeof(T) == 4 ? 2 : 1) k_stage2d(const StageArgs a) {
   using G = typename GeoFor<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red32[32];
@@ -804,8 +816,10 @@ int launch_pipe(const StageArgs& a, cudaStream_t s) {
 // cheap this step (finished, or failed) leave no CTA idle; each grid keeps its
 // own dt, step record and error word, and the CTA that finishes the last tile
 // of a grid in stage 2 plans that grid's next step.
+// FP32-mixed: two CTAs per SM (registers capped at 112 for 288 threads) hide
+// the latency of the FP64 load and update phases behind each other's work
 template <class T, int FLUX, class G>
-__global__ void __launch_bounds__(G::NT) k_batch2d(const StageArgs* __restrict__ args,
+__global__ void __launch_bounds__(G::NT, sizeof(T) == 4 ? 2 : 1) k_batch2d(const StageArgs* __restrict__ args,
                                                    const int* __restrict__ tile_start, int ngrids, int total_tiles,
                                                    int* __restrict__ queue) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
