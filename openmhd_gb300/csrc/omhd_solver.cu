@@ -168,6 +168,22 @@ __global__ void k_bc_axis_s(double* __restrict__ U, int ix, int jx, int kx, int 
   }
 }
 
+// CFL speed of one cell from its conserved variables (set_dt.f90:27-37)
+__device__ __forceinline__ double cell_cfl_speed(const double (&u)[NV], double gamma, int nd) {
+  const double f1g = gamma - 1;
+  const double ro = u[RO];
+  const double mx = u[MX], my = u[MY], mz = u[MZ];
+  const double vx = mx / ro, vy = my / ro, vz = mz / ro;
+  const double rv2 = vx * mx + vy * my + vz * mz;
+  const double bx = u[BX], by = u[BY], bz = u[BZ];
+  const double B2 = bx * bx + by * by + bz * bz;
+  const double pr = f1g * (u[EN] - 0.5 * (rv2 + B2));
+  const double f1 = gamma * pr;
+  double sp = fmax2(fabs(vx) + fast_speed(f1, B2, bx, ro), fabs(vy) + fast_speed(f1, B2, by, ro));
+  if (nd == 3) sp = fmax2(sp, fabs(vz) + fast_speed(f1, B2, bz, ro));
+  return sp;
+}
+
 // CFL speed of the current state (set_dt.f90:27-52) + device step planning
 __global__ void k_init_cfl(const double* __restrict__ U, int ix, int jx, int kx, int nd, double gamma,
                            StepState* st, DevError* err, StepConsts sc) {
@@ -175,23 +191,15 @@ __global__ void k_init_cfl(const double* __restrict__ U, int ix, int jx, int kx,
   const int ni = ix - 2, nj = jx - 2, nk = (nd == 3) ? kx - 2 : 1;
   const long long total = (long long)ni * nj * nk;
   const size_t n = (size_t)ix * jx * kx;
-  const double f1g = gamma - 1;
   double v = 0.0;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
     const int i = 1 + (int)(t % ni), j = 1 + (int)((t / ni) % nj), k = (nd == 3 ? 1 : 0) + (int)(t / ((long long)ni * nj));
     const size_t c = (size_t)i + (size_t)ix * ((size_t)j + (size_t)jx * k);
-    const double ro = U[RO * n + c];
-    const double mx = U[MX * n + c], my = U[MY * n + c], mz = U[MZ * n + c];
-    const double vx = mx / ro, vy = my / ro, vz = mz / ro;
-    const double rv2 = vx * mx + vy * my + vz * mz;
-    const double bx = U[BX * n + c], by = U[BY * n + c], bz = U[BZ * n + c];
-    const double B2 = bx * bx + by * by + bz * bz;
-    const double pr = f1g * (U[EN * n + c] - 0.5 * (rv2 + B2));
-    const double f1 = gamma * pr;
-    double s = fmax2(fabs(vx) + fast_speed(f1, B2, bx, ro), fabs(vy) + fast_speed(f1, B2, by, ro));
-    if (nd == 3) s = fmax2(s, fabs(vz) + fast_speed(f1, B2, bz, ro));
-    v = fmax2(s, v);
+    double u[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) u[q] = U[q * n + c];
+    v = fmax2(cell_cfl_speed(u, gamma, nd), v);
   }
   const double bm = block_max_pos(v, red32);
   reduce_and_finalize(st, sc, err, bm, gridDim.x, 0);
@@ -205,7 +213,6 @@ __global__ void k_upload_cfl(const double* __restrict__ Uh, double* __restrict__
                              double gamma, StepState* st, DevError* err, StepConsts sc) {
   __shared__ double red32[32];
   const size_t n = (size_t)ix * jx * kx;
-  const double f1g = gamma - 1;
   double v = 0.0;
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
     double u[NV];
@@ -216,18 +223,7 @@ __global__ void k_upload_cfl(const double* __restrict__ Uh, double* __restrict__
     }
     const int i = (int)(c % ix), j = (int)((c / ix) % jx), k = (int)(c / ((size_t)ix * jx));
     const bool interior = i >= 1 && i <= ix - 2 && j >= 1 && j <= jx - 2 && (nd != 3 || (k >= 1 && k <= kx - 2));
-    if (!interior) continue;
-    const double ro = u[RO];
-    const double mx = u[MX], my = u[MY], mz = u[MZ];
-    const double vx = mx / ro, vy = my / ro, vz = mz / ro;
-    const double rv2 = vx * mx + vy * my + vz * mz;
-    const double bx = u[BX], by = u[BY], bz = u[BZ];
-    const double B2 = bx * bx + by * by + bz * bz;
-    const double pr = f1g * (u[EN] - 0.5 * (rv2 + B2));
-    const double f1 = gamma * pr;
-    double sp = fmax2(fabs(vx) + fast_speed(f1, B2, bx, ro), fabs(vy) + fast_speed(f1, B2, by, ro));
-    if (nd == 3) sp = fmax2(sp, fabs(vz) + fast_speed(f1, B2, bz, ro));
-    v = fmax2(sp, v);
+    if (interior) v = fmax2(cell_cfl_speed(u, gamma, nd), v);
   }
   const double bm = block_max_pos(v, red32);
   reduce_and_finalize(st, sc, err, bm, gridDim.x, 0);
@@ -315,8 +311,11 @@ StepConsts consts_of(const omhd_solver* s) {
   return StepConsts{s->cfg.cfl, s->dmin, s->cfg.dx, s->cfg.eta_kind};
 }
 
-int launch_stage(omhd_solver* s, int stage) {
-  const StageArgs a = make_stage_args(s, stage);
+// one stage of the current step; Uhost (stage 2 only): the result is also
+// written to this device address of page-locked host memory
+int launch_stage(omhd_solver* s, int stage, double* Uhost = nullptr) {
+  StageArgs a = make_stage_args(s, stage);
+  a.Uhost = Uhost;
   const omhd_config& c = s->cfg;
   int e;
   if (c.nd == 2) {
@@ -588,23 +587,7 @@ int omhd_solver_step_host(omhd_solver* s, const double* U_in, double* U_out, dou
   double* dout = mapped_host(U_out);
   for (int k = 0; k < nsteps; ++k) {
     r = launch_stage(s, 1);
-    if (r) return r;
-    if (k == nsteps - 1 && dout) {
-      StageArgs a = make_stage_args(s, 2);
-      a.Uhost = dout;
-      int e;
-      if (c.nd == 2)
-        e = (c.precision == OMHD_PREC_FP64)          ? launch_stage2d_fp64(a, s->stream)
-            : (c.precision == OMHD_PREC_FP64_PARITY) ? launch_stage2d_parity(a, s->stream)
-                                                     : launch_stage2d_mixed(a, s->stream);
-      else
-        e = (c.precision == OMHD_PREC_FP64)          ? launch_stage3d_fp64(a, s->stream)
-            : (c.precision == OMHD_PREC_FP64_PARITY) ? launch_stage3d_parity(a, s->stream)
-                                                     : launch_stage3d_mixed(a, s->stream);
-      r = cerr(s, (cudaError_t)e, "stage kernel launch");
-    } else {
-      r = launch_stage(s, 2);
-    }
+    if (!r) r = launch_stage(s, 2, k == nsteps - 1 ? dout : nullptr);
     if (r) return r;
   }
   StepState after;
