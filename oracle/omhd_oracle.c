@@ -1,7 +1,7 @@
 /*
  * omhd_oracle.c -- CPU restatement of OpenMHD's finite-volume MHD step.
  *
- * TEST INFRASTRUCTURE ONLY (the checker).  The product never links or calls
+ * TEST INFRASTRUCTURE ONLY (the oracle).  The product never links or calls
  * this file; tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs
  * do.  Parity status: UNPINNED (the reference ships no golden vectors and no
  * Fortran compiler is available to run it); see omhd_oracle.h.

@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product (openmhd_gb300/) links,
  * loads or calls this code; only tests/, __graft_entry__.smoke() and the
- * CPU-baseline legs of bench.py use it, as the checker.
+ * CPU-baseline legs of bench.py use it, to check results against.
  *
  * Parity status: UNPINNED.  The reference (zenitani/OpenMHD) is Fortran 90,
  * ships no tests, fixtures or golden vectors, and no Fortran compiler exists

@@ -1,7 +1,7 @@
 """ctypes front end of the CPU oracle (oracle/omhd_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
-CPU-baseline legs of bench.py as the checker.  The product (openmhd_gb300/)
+CPU-baseline legs of bench.py, to check results against.  The product (openmhd_gb300/)
 never imports it.  Parity status: unpinned (no reference golden vectors exist
 and no Fortran compiler is available to run the reference itself).
 

@@ -1,4 +1,4 @@
-"""CPU checks of the oracle (the checker itself): golden fixtures, HLLD branch
+"""CPU checks of the oracle itself: golden fixtures, HLLD branch
 coverage, limiter known answers, conservation and symmetry properties."""
 import math
 import os
