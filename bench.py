@@ -38,8 +38,8 @@ WORKLOAD = "kh2d_4096x2048_hlld_minmod_glm_tvdrk2"
 BYTES_PER_CELL_UPDATE_2D = 45 * 8  # stage 1: read U, write U1; stage 2: read U, U1, write U
 
 
-def _load_flops():
-    p = os.path.join(ROOT, "profiles", "flops_kh2d.txt")
+def _load_flops(name: str = "flops_kh2d.txt"):
+    p = os.path.join(ROOT, "profiles", name)
     if os.path.exists(p):
         m = re.search(r"flops_per_cell_update:\s*([0-9.]+)", open(p).read())
         if m:
@@ -330,6 +330,8 @@ def run_ours(args):
         line["adjoint"] = run_adjoint(args)
     if not args.no_3d:
         line["harris3d"] = run_3d(args)
+    if not args.no_sq:
+        line["ot4096sq"] = run_sq4096(args, fp64_peak)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"], _ = cpu_baseline(steps_budget_s=10.0)
     if rank == 0:
@@ -406,6 +408,44 @@ def run_batched(args):
             "steps_compared": total_steps, "max_member_scaled_l1_vs_fp64": max(errs),
             "median_member_scaled_l1_vs_fp64": float(np.median(errs)),
             "dt_range": [min(x.dt for x in infos), max(x.dt for x in infos)]}
+
+
+def run_sq4096(args, fp64_peak_gflops: float):
+    """Orszag-Tang 4096 x 4096 (HLLD + MC + GLM + TVD-RK2, periodic), FP64: the
+    square grid the FP64 roofline target is stated on.  Throughput and the
+    fraction of the FP64 DFMA peak from the flop count of this workload
+    (profiles/flops_ot2d_4096x4096.txt); the state (1.21 GB) is larger than L2."""
+    import torch
+
+    from openmhd_gb300 import Solver, orszag_tang
+
+    steps = max(3, min(args.steps, 20))
+    warm = 3
+    cfg, model = orszag_tang(4096, precision="fp64")
+    s = Solver(cfg).init_model(model)
+    s.step(warm)
+    s.sync()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s.stream)
+    s.step(steps)
+    e1.record(s.stream)
+    e1.synchronize()
+    info = s.sync()
+    t = e0.elapsed_time(e1) / 1e3
+    cells = cfg.interior_cells
+    flops_cu = _load_flops("flops_ot2d_4096x4096.txt")
+    ach = flops_cu * cells * steps / t / 1e12
+    out = {"workload": "ot2d_4096x4096_hlld_mc_glm_tvdrk2", "steps": steps, "warmup": warm,
+           "value": cells * steps / t, "unit": "cell-updates/s", "ms_per_step": 1e3 * t / steps,
+           "status": info.status, "steps_done": info.steps,
+           "roofline": {"bound": "fp64", "achieved": ach, "peak": fp64_peak_gflops / 1e3, "unit": "TFLOP/s",
+                        "frac": ach / (fp64_peak_gflops / 1e3), "flops_per_cell_update": flops_cu,
+                        "timing": "whole step (both stage launches and the step planning)"}}
+    del s
+    torch.cuda.empty_cache()
+    return out
 
 
 H3_NX, H3_NY, H3_NZ = 512, 256, 512
@@ -699,6 +739,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-3d", action="store_true")
+    ap.add_argument("--no-sq", action="store_true", help="skip the Orszag-Tang 4096x4096 FP64 leg")
     ap.add_argument("--adjoint-only", action="store_true", help="run the adjoint leg alone")
     ap.add_argument("--profile", action="store_true", help="small fixed run for profiler captures")
     ap.add_argument("--profile-adjoint", action="store_true", help="small adjoint run for profiler captures")

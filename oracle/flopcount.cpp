@@ -27,6 +27,7 @@ inline cd operator-(cd a, cd b) { ++g_flops; return cd(a.v - b.v); }
 inline cd operator*(cd a, cd b) { ++g_flops; return cd(a.v * b.v); }
 inline cd operator/(cd a, cd b) { ++g_flops; return cd(a.v / b.v); }
 inline cd operator-(cd a) { return cd(-a.v); }
+inline cd operator+(cd a) { return a; }
 inline cd& operator+=(cd& a, cd b) { ++g_flops; a.v += b.v; return a; }
 inline bool operator<(cd a, cd b) { return a.v < b.v; }
 inline bool operator>(cd a, cd b) { return a.v > b.v; }

@@ -53,6 +53,31 @@ def test_orszag_tang_vs_oracle(cuda_lib, oracle_mod, precision, tol1, tolN):
     _cmp(s, g, tolN, "10 steps")
 
 
+def test_orszag_tang_4096sq_fp64_vs_oracle(cuda_lib, oracle_mod):
+    """The FP64 gate at the 4096^2 size: Orszag-Tang 4096x4096 (HLLD, MC, GLM,
+    periodic) on the performance build, 1 step within 1e-12 and 10 steps within
+    1e-9 scaled L1 per variable of the oracle (its OpenMP build, which runs the
+    same loops as the serial one), from the same initial state."""
+    from openmhd_gb300 import Solver, orszag_tang
+    from oracle.oracle import Grid
+
+    cfg, model = orszag_tang(4096, precision="fp64")
+    assert (cfg.limiter, cfg.flux) == ("mc", "hlld")
+    s = Solver(cfg).init_model(model)
+    g = Grid.from_solver_config(cfg, omp=True)
+    g.U[...] = s.get_state_numpy()
+    s.step(1)
+    info = s.sync()
+    g.step(1)
+    assert info.status == 0 and abs(info.dt - g.last_dt) <= 1e-14 * g.last_dt
+    _cmp(s, g, 1e-12, "4096^2, 1 step")
+    s.step(9)
+    info = s.sync()
+    g.step(9)
+    assert info.status == 0 and info.steps == 10
+    _cmp(s, g, 1e-9, "4096^2, 10 steps")
+
+
 @pytest.mark.parametrize("flux", ["llf", "hll", "hllc", "hlld", "lhlld"])
 @pytest.mark.parametrize("limiter", ["flat", "minmod", "mc", "vanleer", "koren"])
 def test_scheme_matrix_parity(cuda_lib, oracle_mod, flux, limiter):

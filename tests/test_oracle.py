@@ -191,3 +191,21 @@ def test_more_problem_setups(oracle_mod):
     assert np.all(g.U[0] == 1.0) and np.all(g.U[1] == 1.0) and np.all(g.U[2] == 2.0)
     Bmag = np.sqrt((g.U[5:8] ** 2).sum(axis=0))
     assert 5e-4 < Bmag.max() < 5e-3 and np.mean(Bmag == 0.0) > 0.5  # a loop in a field-free box
+
+
+def test_flop_counting_build(tmp_path):
+    """The flop-counting build of the oracle (oracle/flopcount.cpp) compiles
+    and counts a plausible per-cell-update cost on both 2D workloads (about
+    1.8-1.9 k flops: four HLLD faces, the limiters, u2v, RK and CFL)."""
+    import os
+    import re
+    import subprocess
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / "flopcount")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-o", exe,
+                    os.path.join(root, "oracle", "flopcount.cpp")], check=True)
+    for args in (["64", "32", "2"], ["48", "48", "2", "ot"]):
+        out = subprocess.run([exe] + args, check=True, capture_output=True, text=True).stdout
+        f = float(re.search(r"flops_per_cell_update:\s*([0-9.]+)", out).group(1))
+        assert 1500.0 < f < 2300.0, (args, f)
