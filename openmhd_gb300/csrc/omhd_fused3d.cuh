@@ -60,6 +60,12 @@ __device__ __forceinline__ double eta3(int kind, double x, double y, double z) {
   return 0.0;
 }
 
+// eta / dx of the Harris resistivity, eta = 1e-3 + exp(-(x^2+z^2)/4)/60, from
+// the factors ex = exp(-x^2/4) and ez = exp(-z^2/4)
+__device__ __forceinline__ double harris_eta_dx(double ex, double ez, double inv_dx) {
+  return (1.0e-3 + (1.0 / 60.0) * (ex * ez)) * inv_dx;
+}
+
 // Load + convert one z plane (global index gk, any value; mapped by the z bc)
 // of the halo tile into ring slot `slot`.
 template <class T>
@@ -108,8 +114,11 @@ __device__ __forceinline__ void load_plane(const StageArgs& a, T* W, int slot, i
   }
 }
 
+// FP32 face arithmetic: two CTAs per SM (registers capped at 128, 97 KB of
+// shared memory each), so that one CTA's FP64 loads, updates and barriers
+// overlap the other's face work.
 template <class T, int FLUX>
-__global__ void __launch_bounds__(NT) k_stage3d(const StageArgs a) {
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const StageArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* W = reinterpret_cast<T*>(smem_raw);  // [NRING][NV][PL]
   T* SL = W + NRING * NV * PL;
@@ -146,6 +155,27 @@ __global__ void __launch_bounds__(NT) k_stage3d(const StageArgs a) {
   auto slot = [](int k) { return ((k % NRING) + NRING) % NRING; };
   auto Wv = [&](int k, int v, int o) -> T { return W[(size_t)slot(k) * NV * PL + v * PL + o]; };
 
+  // The Harris resistivity is separable in x and z: in the FAST builds its
+  // exponential is tabulated over this CTA's x columns (cell centres ex_c and
+  // x faces ex_f, index q = i - gi0 + 1) and z chunk (ez_c, ez_f at z faces,
+  // index p = k - k0 + 1), one exp per entry instead of one per face.
+  __shared__ double ex_c[TX + 2], ex_f[TX + 2], ez_c[ZCHUNK + 2], ez_f[ZCHUNK + 2];
+  const bool sep_eta = OMHD_FAST && a.eta_kind == OMHD_ETA_HARRIS_XZ;
+  const double inv_dx = 1.0 / a.dx;
+  if (sep_eta) {
+    for (int q = tid; q < 2 * (TX + 2) + 2 * (ZCHUNK + 2); q += NT) {
+      if (q < 2 * (TX + 2)) {
+        const int p = q % (TX + 2);
+        const double x = a.xc[min(gi0 - 1 + p, ix - 1)] + (q >= TX + 2 ? 0.5 * a.dx : 0.0);
+        (q < TX + 2 ? ex_c : ex_f)[p] = exp(-(x * x) / 4.0);
+      } else {
+        const int r = q - 2 * (TX + 2), p = r % (ZCHUNK + 2);
+        const double z = a.zc[min(k0 - 1 + p, kx - 1)] + (r >= ZCHUNK + 2 ? 0.5 * a.dx : 0.0);
+        (r < ZCHUNK + 2 ? ez_c : ez_f)[p] = exp(-(z * z) / 4.0);
+      }
+    }
+  }
+
   // ---- prologue: planes k0-2 .. k0+1, z face k0-1/2, cached upper state of cell k0 ----
   for (int p = k0 - 2; p <= k0 + 1; ++p)
     load_plane<T>(a, W, slot(p), p, gi0, gj0, perx, pery, perz, resist, glmf, p == k0);
@@ -157,9 +187,9 @@ __global__ void __launch_bounds__(NT) k_stage3d(const StageArgs a) {
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       T l, r;
-      reconstruct<T>(lm, Wv(k0 - 2, v, oc), Wv(k0 - 1, v, oc), Wv(k0, v, oc), l, r);
+      reconstruct_t<T, OMHD_FAST>(lm, Wv(k0 - 2, v, oc), Wv(k0 - 1, v, oc), Wv(k0, v, oc), l, r);
       L[v] = l;  // upper state of cell k0-1
-      reconstruct<T>(lm, Wv(k0 - 1, v, oc), Wv(k0, v, oc), Wv(k0 + 1, v, oc), l, r);
+      reconstruct_t<T, OMHD_FAST>(lm, Wv(k0 - 1, v, oc), Wv(k0, v, oc), Wv(k0 + 1, v, oc), l, r);
       R[v] = r;  // lower state of cell k0
       sLc[v] = l;
     }
@@ -173,7 +203,8 @@ __global__ void __launch_bounds__(NT) k_stage3d(const StageArgs a) {
     if (resist && own) {  // z face k0-1/2 (flux_resistive.cuf:121-135)
       const int k = k0 - 1;
       auto B = [&](int var, int dxo, int dyo, int dzo) { return double(Wv(k + dzo, var, oc + dxo + dyo * RX)); };
-      const double eta_dx = eta3(a.eta_kind, a.xc[gi], a.yc[gj], a.zc[k] + 0.5 * a.dx) / a.dx;
+      const double eta_dx = sep_eta ? harris_eta_dx(ex_c[tx + 1], ez_f[0], inv_dx)
+                                    : eta3(a.eta_kind, a.xc[gi], a.yc[gj], a.zc[k] + 0.5 * a.dx) / a.dx;
       const double JyS = (B(BX, 0, 0, 1) - B(BX, 0, 0, 0)) -
                          0.25 * (B(BZ, 1, 0, 0) + B(BZ, 1, 0, 1) - B(BZ, -1, 0, 0) - B(BZ, -1, 0, 1));
       const double JxS = -(B(BY, 0, 0, 1) - B(BY, 0, 0, 0)) +
@@ -214,7 +245,7 @@ __global__ void __launch_bounds__(NT) k_stage3d(const StageArgs a) {
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
         T l, r;
-        reconstruct<T>(lm, Wk[v * PL + o - 1], Wk[v * PL + o], Wk[v * PL + o + 1], l, r);
+        reconstruct_t<T, OMHD_FAST>(lm, Wk[v * PL + o - 1], Wk[v * PL + o], Wk[v * PL + o + 1], l, r);
         SL[v * SFACE + q] = l;
         SR[v * SFACE + q] = r;
       }
@@ -249,7 +280,8 @@ __global__ void __launch_bounds__(NT) k_stage3d(const StageArgs a) {
         if (g >= 0 && g <= ix - 2 && gjj <= jx - 2) {
           const int o = (cy + 2) * RX + (fx + 1);
           auto B = [&](int var, int dxo, int dyo, int dzo) { return double(Wv(k + dzo, var, o + dxo + dyo * RX)); };
-          const double eta_dx = eta3(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gjj], a.zc[k]) / a.dx;
+          const double eta_dx = sep_eta ? harris_eta_dx(ex_f[fx], ez_c[k - k0 + 1], inv_dx)
+                                        : eta3(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gjj], a.zc[k]) / a.dx;
           const double JyS = -(B(BZ, 1, 0, 0) - B(BZ, 0, 0, 0)) +
                              0.25 * (B(BX, 0, 0, 1) + B(BX, 1, 0, 1) - B(BX, 0, 0, -1) - B(BX, 1, 0, -1));
           const double JzS = (B(BY, 1, 0, 0) - B(BY, 0, 0, 0)) -
@@ -276,7 +308,7 @@ __global__ void __launch_bounds__(NT) k_stage3d(const StageArgs a) {
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
         T l, r;
-        reconstruct<T>(lm, Wk[v * PL + o - RX], Wk[v * PL + o], Wk[v * PL + o + RX], l, r);
+        reconstruct_t<T, OMHD_FAST>(lm, Wk[v * PL + o - RX], Wk[v * PL + o], Wk[v * PL + o + RX], l, r);
         SL[v * SFACE + q] = l;
         SR[v * SFACE + q] = r;
       }
@@ -312,7 +344,8 @@ __global__ void __launch_bounds__(NT) k_stage3d(const StageArgs a) {
         if (g >= 0 && g <= jx - 2 && gii <= ix - 2) {
           const int o = (fy + 1) * RX + (cx + 2);
           auto B = [&](int var, int dxo, int dyo, int dzo) { return double(Wv(k + dzo, var, o + dxo + dyo * RX)); };
-          const double eta_dx = eta3(a.eta_kind, a.xc[gii], a.yc[g] + 0.5 * a.dx, a.zc[k]) / a.dx;
+          const double eta_dx = sep_eta ? harris_eta_dx(ex_c[cx + 1], ez_c[k - k0 + 1], inv_dx)
+                                        : eta3(a.eta_kind, a.xc[gii], a.yc[g] + 0.5 * a.dx, a.zc[k]) / a.dx;
           const double JxS = (B(BZ, 0, 1, 0) - B(BZ, 0, 0, 0)) -
                              0.25 * (B(BY, 0, 0, 1) + B(BY, 0, 1, 1) - B(BY, 0, 0, -1) - B(BY, 0, 1, -1));
           const double JzS = -(B(BX, 0, 1, 0) - B(BX, 0, 0, 0)) +
@@ -341,7 +374,7 @@ __global__ void __launch_bounds__(NT) k_stage3d(const StageArgs a) {
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
         T l, r;
-        reconstruct<T>(lm, Wv(k, v, oc), Wv(k + 1, v, oc), Wv(k + 2, v, oc), l, r);
+        reconstruct_t<T, OMHD_FAST>(lm, Wv(k, v, oc), Wv(k + 1, v, oc), Wv(k + 2, v, oc), l, r);
         L[v] = sLc[v];
         R[v] = r;
         sLn[v] = l;
@@ -355,7 +388,8 @@ __global__ void __launch_bounds__(NT) k_stage3d(const StageArgs a) {
       for (int v = 0; v < NV; ++v) Fzc[v] = double(Fo[v]);
       if (resist && own) {  // flux_resistive.cuf:121-135
         auto B = [&](int var, int dxo, int dyo, int dzo) { return double(Wv(k + dzo, var, oc + dxo + dyo * RX)); };
-        const double eta_dx = eta3(a.eta_kind, a.xc[gi], a.yc[gj], a.zc[k] + 0.5 * a.dx) / a.dx;
+        const double eta_dx = sep_eta ? harris_eta_dx(ex_c[tx + 1], ez_f[k - k0 + 1], inv_dx)
+                                      : eta3(a.eta_kind, a.xc[gi], a.yc[gj], a.zc[k] + 0.5 * a.dx) / a.dx;
         const double JyS = (B(BX, 0, 0, 1) - B(BX, 0, 0, 0)) -
                            0.25 * (B(BZ, 1, 0, 0) + B(BZ, 1, 0, 1) - B(BZ, -1, 0, 0) - B(BZ, -1, 0, 1));
         const double JxS = -(B(BY, 0, 0, 1) - B(BY, 0, 0, 0)) +

@@ -245,6 +245,42 @@ def test_harris3d_resistive_vs_oracle(cuda_lib, oracle_mod, precision, tol):
     _cmp(s, g, tol, "harris3d")
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64_parity", 1e-12), ("fp64", 1e-10)])
+def test_harris3d_resistive_multichunk_vs_oracle(cuda_lib, oracle_mod, precision, tol):
+    """Resistive Harris sheet on 136x68x136 (dx = dy = dz): five CTA columns
+    across x (one ragged) and three z chunks, with the resistivity peak at
+    x = z = 0 inside the third column and the second chunk, so the resistivity
+    at the face positions of a column and chunk away from the origin
+    (tabulated per CTA in the FAST builds) meets the oracle's per-face
+    formula."""
+    from openmhd_gb300 import harris3d
+
+    cfg, model = harris3d(136, 68, 136, precision=precision)
+    s, g = _pair(cfg, model, oracle_mod)
+    s.step(3)
+    info = s.sync()
+    g.step(3)
+    assert info.status == 0 and info.steps == 3
+    _cmp(s, g, tol, "harris3d multichunk")
+
+
+def test_harris3d_mixed_error_vs_fp64(cuda_lib):
+    """FP32-mixed 3D (resistive Harris sheet 136x68x136, two CTAs per SM)
+    within 1e-6 scaled L1 per variable of the FP64 path after 10 steps."""
+    from openmhd_gb300 import Solver, harris3d
+
+    cfg64, model = harris3d(136, 68, 136, precision="fp64")
+    cfgmx, _ = harris3d(136, 68, 136, precision="mixed")
+    a = Solver(cfg64).init_model(model)
+    b = Solver(cfgmx).init_model(model)
+    a.step(10)
+    b.step(10)
+    ia, ib = a.sync(), b.sync()
+    assert ia.status == 0 and ib.status == 0 and ia.steps == ib.steps == 10
+    err = scaled_l1(interior(b.get_state_numpy()), interior(a.get_state_numpy()))
+    assert np.all(err <= 1e-6), err
+
+
 def test_3d_periodic_multichunk_vs_oracle(cuda_lib, oracle_mod):
     """Random smooth periodic 3D state with more z planes than one CTA marches
     (chunk boundaries), MC limiter, no resistivity."""
