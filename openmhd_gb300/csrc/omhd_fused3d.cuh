@@ -299,7 +299,9 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
 #pragma unroll
     for (int v = 0; v < NV; ++v)
       acc[v] = double(FB[v * SFLUX + ty * XF + tx]) - double(FB[v * SFLUX + ty * XF + tx + 1]);
-    __syncthreads();
+    // no barrier here: the y reconstruction writes only SL/SR (last read by the
+    // x fluxes, before the barrier above), and FB is next written by the y
+    // fluxes, after the barrier that follows the y reconstruction
 
     // ---- y pass on plane k ----
     for (int q = tid; q < (TY + 2) * TX; q += NT) {
