@@ -1,0 +1,45 @@
+"""The JSON line of bench.py's reference arm (the CPU restatement of the
+reference's serial path, timed on the host cores): its keys and values, on a
+small KH grid so that it runs on any machine."""
+import argparse
+import json
+
+import pytest
+
+
+@pytest.fixture
+def small_baseline(monkeypatch, oracle_mod):
+    import bench
+
+    orig = bench.cpu_baseline
+    monkeypatch.setenv("OMP_NUM_THREADS", "1")
+    monkeypatch.setattr(bench, "cpu_baseline",
+                        lambda steps_budget_s=1.0, omp=True, nx=0, ny=0: orig(steps_budget_s=0.2, omp=False,
+                                                                              nx=64, ny=32))
+    return bench
+
+
+def test_reference_arm_line(small_baseline, capsys, monkeypatch):
+    monkeypatch.delenv("RANK", raising=False)
+    rc = small_baseline.run_reference(argparse.Namespace(gpus=1, steps=2, warmup=3))
+    assert rc == 0
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    assert line["metric"] == "cell-updates/s" and line["unit"] == "cell-updates/s"
+    assert line["value"] > 0 and line["higher_is_better"] is True
+    assert (line["n_gpus"], line["steps"], line["warmup"]) == (1, 2, 3)
+    assert line["scaling"] == "weak" and line["vs_baseline"] is None and line["dtype"] == "f64"
+    assert line["config"]["workload"] == small_baseline.WORKLOAD
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] == 1 and cb["value"] == line["value"]
+    assert "64x32" in cb["sample"]
+    e2e = line["e2e"]
+    assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
+    assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_other_ranks_print_nothing(small_baseline, capsys, monkeypatch):
+    monkeypatch.setenv("RANK", "1")
+    monkeypatch.setenv("WORLD_SIZE", "2")
+    assert small_baseline.run_reference(argparse.Namespace(gpus=2, steps=2, warmup=3)) == 0
+    assert capsys.readouterr().out == ""
