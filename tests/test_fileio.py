@@ -89,3 +89,39 @@ def test_solver_snapshot_and_restart(cuda_lib, tmp_path, oracle_mod):
     ia, ib = a.sync(), b.sync()
     assert ia.t == ib.t
     assert np.array_equal(a.get_state_numpy(), b.get_state_numpy())
+
+
+def test_layout_pinned_by_reference_readers(lib, tmp_path):
+    """The files written for the seeded states of tests/golden/make_fileio_golden.py
+    are byte for byte the files that the reference's own readers
+    (visualization/openmhd2d.py, openmhd3d.py) parsed into the recorded arrays,
+    those arrays are the written state, and our reader returns the same."""
+    import os
+    import sys
+
+    from openmhd_gb300 import fileio
+
+    golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, golden)
+    import make_fileio_golden as G
+
+    rec = np.load(os.path.join(golden, "fileio_reference_reader.npz"))
+    for nd in (2, 3):
+        path = str(tmp_path / f"field-0000{nd}.dat")
+        assert G.write_case(nd, path) == str(rec[f"sha256_{nd}d"])
+        t, x, y, z, U, V = G.seeded_case(nd)
+        field = (lambda a: a.T) if nd == 2 else (lambda a: a.transpose(2, 1, 0))
+        data = rec[f"data_{nd}d"]
+        assert float(rec[f"t_{nd}d"]) == t
+        assert np.array_equal(rec[f"x_{nd}d"], x) and np.array_equal(rec[f"y_{nd}d"], y)
+        if nd == 3:
+            assert np.array_equal(rec["z_3d"], z)
+        for q in range(4):
+            assert np.array_equal(data[..., q], field(V[q]))
+        for q in range(4, 9):
+            assert np.array_equal(data[..., q], field(U[q]))
+        shape = G.SHAPES[nd]
+        t2, x2, y2, z2, U2 = fileio.read(path, nd, shape[-1], shape[-2], shape[0] if nd == 3 else 1)
+        assert t2 == t and np.array_equal(U2, U) and np.array_equal(x2, x) and np.array_equal(y2, y)
+        if nd == 3:
+            assert np.array_equal(z2, z)
