@@ -58,3 +58,27 @@ def test_product_does_not_reference_oracle():
                 src = open(os.path.join(dirpath, f)).read()
                 assert "import oracle" not in src and "from oracle" not in src, f
                 assert "omhd_oracle" not in src, f
+
+
+def test_plain_c_program_links_every_symbol(lib, tmp_path):
+    """A C99 program that includes the header, takes the address of every
+    declared function and calls omhd_abi_version() compiles with -pedantic
+    -Werror, links against libopenmhd_gb300.so and runs without a GPU: the
+    header is the ABI a Fortran or C driver links to."""
+    import subprocess
+
+    names = declared_functions()
+    src = tmp_path / "abi.c"
+    src.write_text(
+        '#include <stdio.h>\n#include "openmhd_gb300.h"\n'
+        "typedef void (*fn)(void);\n"
+        "static const fn table[] = {\n" + ",\n".join(f"  (fn){n}" for n in names) + "\n};\n"
+        "int main(void) {\n"
+        '  printf("%d %d\\n", omhd_abi_version(), (int)(sizeof table / sizeof table[0]));\n'
+        "  return 0;\n}\n")
+    libdir = os.path.join(ROOT, "openmhd_gb300")
+    exe = tmp_path / "abi"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-L", libdir, "-lopenmhd_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert out == ["1", str(len(names))]
