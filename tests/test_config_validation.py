@@ -1,0 +1,61 @@
+"""omhd_solver_create checks its configuration before it touches the GPU, so
+the rejections run on any machine: bad arguments give OMHD_BAD_ARG (4) and
+resistive runs on unequal spacings OMHD_NOT_SUPPORTED (7), because the
+reference's resistive fluxes use one spacing for every direction
+(2D_reconnection/flux_resistive.f90, 3D_reconnection_gpu/flux_resistive.cuf)."""
+import ctypes as C
+import dataclasses
+
+import pytest
+
+from openmhd_gb300.solver import OMHD_BAD_ARG, OMHD_NOT_SUPPORTED
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from openmhd_gb300 import _lib
+    from openmhd_gb300.build import build
+
+    build()
+    return _lib.load()
+
+
+def _create(lib, cfg):
+    h = C.c_void_p()
+    st = lib.omhd_solver_create(C.byref(cfg.to_c()), C.byref(h))
+    assert not h.value  # nothing is allocated for a rejected configuration
+    return st
+
+
+def test_resistive_needs_equal_spacings(lib):
+    from openmhd_gb300 import harris3d, reconnection2d
+
+    cfg, _ = harris3d(9, 6, 10)  # dx, dy, dz = 22.2, 16.7, 20
+    assert _create(lib, cfg) == OMHD_NOT_SUPPORTED
+    cfg, _ = reconnection2d(12, 6)
+    assert _create(lib, dataclasses.replace(cfg, dy=cfg.dx * 1.5)) == OMHD_NOT_SUPPORTED
+
+
+def test_bad_arguments(lib):
+    from openmhd_gb300 import kelvin_helmholtz, orszag_tang
+
+    cfg, _ = orszag_tang(16)
+    bad = [
+        dataclasses.replace(cfg, ix=3),  # fewer than 2 interior cells
+        dataclasses.replace(cfg, nd=4),
+        dataclasses.replace(cfg, kx=5),  # 2D with a third extent
+        dataclasses.replace(cfg, dx=0.0),
+        dataclasses.replace(cfg, dy=float("nan")),
+    ]
+    kh, _ = kelvin_helmholtz(16, 8)
+    bad.append(dataclasses.replace(kh, bc_kind=(0, 0, 0, 1, 0, 0)))  # periodic on one side only
+    for c in bad:
+        assert _create(lib, c) == OMHD_BAD_ARG, c
+    c = cfg.to_c()
+    h = C.c_void_p()
+    c.lm_type = 5
+    assert lib.omhd_solver_create(C.byref(c), C.byref(h)) == OMHD_BAD_ARG
+    c = cfg.to_c()
+    c.eta_kind = 3
+    assert lib.omhd_solver_create(C.byref(c), C.byref(h)) == OMHD_BAD_ARG
+    assert lib.omhd_solver_create(C.byref(cfg.to_c()), None) == OMHD_BAD_ARG
