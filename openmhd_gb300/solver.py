@@ -19,6 +19,7 @@ OMHD_BAD_ARG = 4  # omhd_status_t
 OMHD_TIMEOUT = 5
 OMHD_CUDA_ERR = 6
 OMHD_NOT_SUPPORTED = 7
+OMHD_IO_ERR = 8
 LIMITERS = {"flat": 0, "minmod": 1, "mc": 2, "vanleer": 3, "koren": 4}
 FLUXES = {"llf": 0, "hll": 1, "hllc": 2, "hlld": 3, "lhlld": 4}
 PRECISIONS = {"fp64": 0, "fp64_parity": 1, "mixed": 2}

@@ -66,6 +66,27 @@ def test_input_rejects_other_sizes(lib, tmp_path):
     assert e.value.code == 4  # OMHD_BAD_ARG, fileio.f90:77-82 "parameter mismatch"
 
 
+def test_input_reports_missing_and_truncated_files(lib, tmp_path):
+    """A missing file and a file cut short in its header, coordinates or planes
+    are reported as OMHD_IO_ERR (the reference's read would stop)."""
+    from openmhd_gb300 import OmhdError, fileio
+    from openmhd_gb300.solver import OMHD_IO_ERR
+
+    U = random_state((6, 7), 2)
+    path = tmp_path / "f.dat"
+    fileio.write(path, 1.0, np.zeros(7), np.zeros(6), U, np.zeros((4, 6, 7)))
+    data = path.read_bytes()
+    with pytest.raises(OmhdError) as e:
+        fileio.read(tmp_path / "missing.dat", 2, 7, 6)
+    assert e.value.code == OMHD_IO_ERR
+    for cut in (4, 8 + 4, 8 + 8 + 7 * 8 + 3, len(data) - 4 * 6 * 7 * 8 - 8):
+        short = tmp_path / f"short{cut}.dat"
+        short.write_bytes(data[:cut])
+        with pytest.raises(OmhdError) as e:
+            fileio.read(short, 2, 7, 6)
+        assert e.value.code == OMHD_IO_ERR, cut
+
+
 @pytest.mark.gpu
 def test_solver_snapshot_and_restart(cuda_lib, tmp_path, oracle_mod):
     from openmhd_gb300 import Solver, orszag_tang
