@@ -99,6 +99,10 @@ int omhd_ensemble_create(const omhd_config* cfgs, int n, omhd_ensemble** out) {
   if (flux != OMHD_FLUX_HLLD) return OMHD_NOT_SUPPORTED;
   for (int i = 0; i < n; ++i)
     if (cfgs[i].nd != 2 || cfgs[i].precision != prec || cfgs[i].flux_type != flux) return OMHD_NOT_SUPPORTED;
+  for (int i = 0; i < n; ++i) {  // every member is checked before anything is allocated
+    const int v = validate_config(&cfgs[i]);
+    if (v) return v;
+  }
   omhd_ensemble* e = new omhd_ensemble();
   e->n = n;
   e->precision = prec;

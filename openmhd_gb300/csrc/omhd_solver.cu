@@ -382,6 +382,10 @@ void drop_graph(omhd_solver* s) {
 
 }  // namespace
 
+namespace omhd {
+int validate_config(const omhd_config* c) { return validate(c); }
+}  // namespace omhd
+
 extern "C" {
 
 int omhd_solver_create(const omhd_config* cfg, omhd_solver** out) {

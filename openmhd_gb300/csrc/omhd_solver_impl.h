@@ -37,4 +37,7 @@ struct omhd_solver {
 namespace omhd {
 // argument block of stage 1 or 2 of a solver's current step
 StageArgs make_stage_args(const omhd_solver* s, int stage);
+// the checks omhd_solver_create makes before any GPU work: OMHD_OK,
+// OMHD_BAD_ARG or OMHD_NOT_SUPPORTED
+int validate_config(const omhd_config* c);
 }  // namespace omhd

@@ -59,3 +59,54 @@ def test_bad_arguments(lib):
     c.eta_kind = 3
     assert lib.omhd_solver_create(C.byref(c), C.byref(h)) == OMHD_BAD_ARG
     assert lib.omhd_solver_create(C.byref(cfg.to_c()), None) == OMHD_BAD_ARG
+
+
+def _cfg_array(cfgs):
+    from openmhd_gb300 import _lib
+
+    arr = (_lib.Config * len(cfgs))()
+    for i, c in enumerate(cfgs):
+        arr[i] = c.to_c()
+    return arr
+
+
+def test_ensemble_checks_every_member_first(lib):
+    from openmhd_gb300 import harris3d, kelvin_helmholtz, orszag_tang
+    from openmhd_gb300.solver import OMHD_BAD_ARG, OMHD_NOT_SUPPORTED
+
+    ot, _ = orszag_tang(32, precision="mixed")
+    kh, _ = kelvin_helmholtz(48, 16, precision="mixed")
+    h = C.c_void_p()
+    cases = [
+        ([ot, dataclasses.replace(kh, ix=3)], OMHD_BAD_ARG),  # a bad member anywhere in the list
+        ([ot, dataclasses.replace(kh, bc_kind=(1, 0, 1, 1, 0, 0))], OMHD_BAD_ARG),
+        ([ot, harris3d(8, 8, 8, precision="mixed")[0]], OMHD_NOT_SUPPORTED),  # 2D members only
+        ([dataclasses.replace(ot, precision="fp64_parity")], OMHD_NOT_SUPPORTED),
+        ([dataclasses.replace(ot, flux="hll")], OMHD_NOT_SUPPORTED),  # the batched kernel is HLLD
+    ]
+    for cfgs, code in cases:
+        assert lib.omhd_ensemble_create(_cfg_array(cfgs), len(cfgs), C.byref(h)) == code, cfgs
+        assert not h.value
+    assert lib.omhd_ensemble_create(_cfg_array([ot]), 0, C.byref(h)) == OMHD_BAD_ARG
+
+
+def test_adjoint_and_noalloc_argument_checks(lib):
+    import numpy as np
+
+    from openmhd_gb300 import _lib, field_loop3d, kelvin_helmholtz
+    from openmhd_gb300.solver import OMHD_BAD_ARG, OMHD_NOT_SUPPORTED
+
+    kh, _ = kelvin_helmholtz(32, 16)
+    h = C.c_void_p()
+    assert lib.omhd_adjoint_create(C.byref(kh.to_c()), 0, 1, C.byref(h)) == OMHD_BAD_ARG
+    assert lib.omhd_adjoint_create(C.byref(kh.to_c()), 10, 0, C.byref(h)) == OMHD_BAD_ARG
+    for c in (dataclasses.replace(kh, limiter="flat"), dataclasses.replace(kh, flux="hllc"),
+              dataclasses.replace(kh, time="rk2"), field_loop3d(8, 8, 8)[0]):
+        assert lib.omhd_adjoint_create(C.byref(c.to_c()), 10, 5, C.byref(h)) == OMHD_NOT_SUPPORTED, c
+    assert not h.value
+    U = np.zeros(8)  # never touched: the configuration is refused first
+    info = _lib.StepInfo()
+    for c in (field_loop3d(8, 8, 8)[0], dataclasses.replace(kh, jx=3),
+              dataclasses.replace(kh, bc_kind=(0, 0, 0, 1, 0, 0))):
+        st = lib.omhd_step2d_noalloc(U.ctypes.data, C.byref(c.to_c()), 0.0, 1, None, C.byref(info))
+        assert st == OMHD_BAD_ARG, c
