@@ -177,6 +177,16 @@ def run_reference(args):
     return 0
 
 
+def _leg(fn, *a):
+    """One of the further legs of the bench line.  A leg that raises is
+    reported under its own key as {"error": ...}; the headline figures, measured
+    before it, still print."""
+    try:
+        return fn(*a)
+    except Exception as e:  # noqa: BLE001 -- any failure of a leg is reported, not hidden
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -325,15 +335,15 @@ def run_ours(args):
                   "steps_compared": args.warmup + args.steps},
     }
     if not args.no_batched:
-        line["batched"] = run_batched(args)
+        line["batched"] = _leg(run_batched, args)
     if not args.no_adjoint:
-        line["adjoint"] = run_adjoint(args)
+        line["adjoint"] = _leg(run_adjoint, args)
     if not args.no_3d:
-        line["harris3d"] = run_3d(args)
+        line["harris3d"] = _leg(run_3d, args)
     if not args.no_sq:
-        line["ot4096sq"] = run_sq4096(args, fp64_peak)
+        line["ot4096sq"] = _leg(run_sq4096, args, fp64_peak)
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"], _ = cpu_baseline(steps_budget_s=10.0)
+        line["cpu_baseline"] = _leg(lambda: cpu_baseline(steps_budget_s=10.0)[0])
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

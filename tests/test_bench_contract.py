@@ -1,6 +1,6 @@
-"""The JSON line of bench.py's reference arm (the CPU restatement of the
-reference's serial path, timed on the host cores): its keys and values, on a
-small KH grid so that it runs on any machine."""
+"""bench.py without a GPU: the JSON line of the reference arm (the CPU
+restatement of the reference's serial path, timed on the host cores), its keys
+and values on a small KH grid, and how a failing further leg is reported."""
 import argparse
 import json
 
@@ -43,3 +43,13 @@ def test_reference_arm_other_ranks_print_nothing(small_baseline, capsys, monkeyp
     monkeypatch.setenv("WORLD_SIZE", "2")
     assert small_baseline.run_reference(argparse.Namespace(gpus=2, steps=2, warmup=3)) == 0
     assert capsys.readouterr().out == ""
+
+
+def test_failing_leg_is_reported_under_its_key():
+    import bench
+
+    def boom(_):
+        raise RuntimeError("leg failed")
+
+    assert bench._leg(boom, None) == {"error": "RuntimeError: leg failed"}
+    assert bench._leg(lambda a, b: a + b, 1, 2) == 3
