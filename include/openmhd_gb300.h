@@ -24,6 +24,15 @@
  *
  * Errors never trap the GPU: kernels record the first failure in a device
  * error word that the host reads.
+ *
+ * Threads: like the reference's single-threaded drivers, the routine-level
+ * entry points share library-global state (stream, error record, host-array
+ * mirrors) and must be called from one thread at a time; so do the calls that
+ * use them internally (omhd_fileio_output with V = NULL, omhd_solver_write)
+ * and omhd_step2d_noalloc, which also keeps its scratch in one static device
+ * array, so that its calls must not overlap on the GPU either.  Solver,
+ * ensemble and adjoint handles are otherwise independent of each other; one
+ * handle must not be used from two threads at once.
  */
 #ifndef OPENMHD_GB300_H
 #define OPENMHD_GB300_H
