@@ -82,3 +82,52 @@ def test_plain_c_program_links_every_symbol(lib, tmp_path):
                     str(src), "-L", libdir, "-lopenmhd_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
     assert out == ["1", str(len(names))]
+
+
+def _c_prototypes():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    protos = {}
+    for ret, name, params in re.findall(r"^\s*(int|void|double|size_t)\s+\**\s*(\w+)\s*\(([^)]*)\)\s*;", text,
+                                        flags=re.M | re.S):
+        plist = [] if params.strip() in ("", "void") else [p.strip() for p in params.split(",")]
+        parsed = []
+        for p in plist:
+            base = "double" if "double" in p else "int" if re.search(r"\bint\b", p) else "other"
+            parsed.append((base, "*" in p or "[" in p))
+        protos[name] = (ret, parsed)
+    return protos
+
+
+def test_fortran_module_matches_c_prototypes():
+    """include/openmhd_gb300.f90 cannot be compiled here (no Fortran compiler),
+    so its bind(C) interfaces are checked against the C header as text: every
+    bound name is declared, functions return int and subroutines void, and each
+    dummy argument has the C parameter's base type and passing mode (VALUE <->
+    by value, arrays and non-VALUE scalars <-> pointers)."""
+    src = open(os.path.join(ROOT, "include", "openmhd_gb300.f90")).read()
+    protos = _c_prototypes()
+    blocks = re.findall(r"^\s*(integer\(c_int\) function|subroutine)\s+\w+\(([^)]*)\)\s*bind\(C,\s*name=\"(\w+)\"\)"
+                        r"(.*?)^\s*end (?:function|subroutine)", src, flags=re.M | re.S | re.I)
+    assert len(blocks) >= 24
+    for kind, args, cname, body in blocks:
+        assert cname in protos, cname
+        ret, params = protos[cname]
+        assert ret == ("int" if kind.startswith("integer") else "void"), cname
+        names = [a.strip() for a in args.split(",") if a.strip()]
+        assert len(names) == len(params), cname
+        decl = {}
+        for line in body.splitlines():
+            m = re.match(r"\s*(integer\(c_int\)|real\(c_double\))([^:]*)::(.*)", line, flags=re.I)
+            if not m:
+                continue
+            base = "int" if m.group(1).lower().startswith("integer") else "double"
+            by_value = "value" in m.group(2).lower()
+            for item in re.findall(r"(\w+)(\([^)]*\))?", m.group(3)):
+                decl[item[0].lower()] = (base, by_value, bool(item[1]))
+        for a, (cbase, cptr) in zip(names, params):
+            base, by_value, is_array = decl[a.lower()]
+            assert base == cbase, (cname, a)
+            assert by_value == (not cptr), (cname, a)
+            if is_array:
+                assert cptr, (cname, a)
