@@ -131,3 +131,36 @@ def test_fortran_module_matches_c_prototypes():
             assert by_value == (not cptr), (cname, a)
             if is_array:
                 assert cptr, (cname, a)
+
+
+# The reference's subroutine argument lists (2D_basic/u2v.f90, limiter.f90,
+# flux_solver.f90, rk.f90, glm_ss2.f90, set_dt.f90, bc.f90;
+# 2D_reconnection/flux_resistive.f90), one letter per argument: d = real(8),
+# i = integer.
+REFERENCE_ARGS = {
+    "u2v_": "ddii",              # u2v(U,V,ix,jx)
+    "limiter_": "dddiiii",       # limiter(wk,wL,wR,ix,jx,dir,type)
+    "flux_solver_": "ddddiiii",  # flux_solver(F,VL,VR,ch,ix,jx,dir,type)
+    "rk_tvd21_": "ddddddii",     # rk_tvd21(wk,wk1,wF,wG,dt,dx,ix,jx)
+    "rk_tvd22_": "ddddddii",
+    "rk_std21_": "ddddddii",
+    "rk_std22_": "dddddii",      # rk_std22(wk,wF,wG,dt,dx,ix,jx)
+    "glm_ss2_": "dddii",         # glm_ss2(U,ch,dt,ix,jx)
+    "set_dt_": "ddddddii",       # set_dt(U,V,vmax,dt,dx,cfl,ix,jx)
+    "bc_": "dii",                # bc(U,ix,jx)
+    "flux_resistive_": "dddddiii",  # flux_resistive(F,U,x,y,dx,ix,jx,dir)
+    "set_dt_resistive_": "ddd",  # set_dt_resistive(dt,dx,cfl)
+}
+
+
+def test_link_level_dropins_take_the_reference_argument_lists():
+    """gfortran passes every argument by reference and calls lowercase names
+    with a trailing underscore: each drop-in returns void and takes, in order,
+    a pointer of the reference argument's type for every argument."""
+    protos = _c_prototypes()
+    for name, kinds in REFERENCE_ARGS.items():
+        ret, params = protos[name]
+        assert ret == "void", name
+        got = "".join("d" if base == "double" else "i" for base, _ in params)
+        assert got == kinds, (name, got)
+        assert all(ptr for _, ptr in params), name
