@@ -209,3 +209,21 @@ def test_flop_counting_build(tmp_path):
         out = subprocess.run([exe] + args, check=True, capture_output=True, text=True).stdout
         f = float(re.search(r"flops_per_cell_update:\s*([0-9.]+)", out).group(1))
         assert 1500.0 < f < 2300.0, (args, f)
+
+
+@pytest.mark.parametrize("problem", ["kh", "harris3d"])
+def test_openmp_build_equals_serial(oracle_mod, monkeypatch, problem):
+    """The OpenMP build of the oracle (the CPU baseline and the 4096^2 parity
+    reference) runs the same loops as the serial build with only min/max
+    reductions across threads, so it gives the same bits."""
+    from openmhd_gb300 import harris3d, kelvin_helmholtz
+
+    monkeypatch.setenv("OMP_NUM_THREADS", "4")
+    cfg, m = kelvin_helmholtz(64, 48) if problem == "kh" else harris3d(16, 8, 16)
+    out = []
+    for omp in (False, True):
+        g = oracle_mod.Grid.from_solver_config(cfg, omp=omp)
+        g.model(m.kind, amp=m.amp, bx0=m.bx0, pert=m.pert, seed=m.seed, beta=m.beta)
+        g.step(3)
+        out.append((g.U.copy(), g.t, g.last_dt))
+    assert np.array_equal(out[0][0], out[1][0]) and out[0][1:] == out[1][1:]
