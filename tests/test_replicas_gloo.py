@@ -34,7 +34,7 @@ def _worker(rank, world, port, times, out):
 def test_two_rank_max_over_ranks():
     world = 2
     port = _free_port()
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()  # no fork of a process that may hold OpenMP threads
     out = mgr.dict()
     times = [0.5, 0.8]
     mp.spawn(_worker, args=(world, port, times, out), nprocs=world, join=True)
