@@ -262,3 +262,34 @@ def test_alfven_wave_second_order_convergence(oracle_mod):
     e32, e64, e128 = run(32), run(64), run(128)
     assert e128 < 2.5e-4
     assert math.log2(e32 / e64) > 1.6 and math.log2(e64 / e128) > 1.8, (e32, e64, e128)
+
+
+def test_alfven_wave_along_z_in_3d(oracle_mod):
+    """The same exact Alfven wave travelling along z through the 3D oracle
+    (4 x 4 x n periodic box, B_z = 1, B_perp = 0.1 (sin, cos)(2 pi (z - t))):
+    second-order convergence of the z-direction flux, limiter and update."""
+    gamma, amp = 5.0 / 3.0, 0.1
+
+    def run(n):
+        dz = 1.0 / n
+        g = oracle_mod.Grid(3, 6, 6, n + 2, dx=dz, dy=dz, dz=dz, z0=-0.5 * dz, cfl=0.4, gamma=gamma,
+                            lm_type=2, flux_type=3)
+
+        def state(t):
+            ph = 2 * math.pi * (g.z - t)
+            b1, b2 = amp * np.sin(ph), amp * np.cos(ph)
+            U = np.zeros(g.shape)
+            U[4] = 1.0
+            U[0], U[1] = -b1[:, None, None], -b2[:, None, None]
+            U[5], U[6], U[7] = b1[:, None, None], b2[:, None, None], 1.0
+            U[3] = (b1**2 + b2**2 + 0.5 + 0.1 / (gamma - 1))[:, None, None]
+            return U
+
+        g.U[...] = state(0.0)
+        g.bc()
+        g.run_until(1.0)
+        return np.abs(g.U[5, 1:-1, 1:-1, 1:-1] - state(g.t)[5, 1:-1, 1:-1, 1:-1]).mean()
+
+    e32, e64, e128 = run(32), run(64), run(128)
+    assert e128 < 2.5e-4
+    assert math.log2(e32 / e64) > 1.6 and math.log2(e64 / e128) > 1.8, (e32, e64, e128)
