@@ -342,7 +342,10 @@ size_t omhd_step2d_noalloc_max_doubles(void);
  * from U on the GPU (u2v.f90), and a failing u2v (negative pressure or
  * density) is returned without writing.  fileio_input reads t, x, y[, z] and
  * U and rejects a file whose sizes differ (fileio.f90:77-82) with
- * OMHD_BAD_ARG.  The reference's readers read these files unchanged.
+ * OMHD_BAD_ARG; a missing or short file gives OMHD_IO_ERR, and the output
+ * arrays may then hold part of the file (omhd_solver_read reads into its own
+ * buffers first, so a failed restart leaves the solver as it was).  The
+ * reference's readers read these files unchanged.
  * ==================================================================== */
 int omhd_fileio_output(const char* path, int nd, int ix, int jx, int kx, double t, const double* x,
                        const double* y, const double* z, const double* U, const double* V);
