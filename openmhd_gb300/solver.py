@@ -367,6 +367,57 @@ class Solver:
                 raise OmhdError(OMHD_TIMEOUT, "run_until made no progress")
             last = info.steps
 
+    def run_with_output(self, tend: float, dtout: float, outdir: str = "data", batch: int = 64) -> list:
+        """The reference driver's time loop with snapshot output (2D_basic/main.f90:36-75):
+        a field file `outdir/field-NNNNN.dat` at the start and then at the first
+        t >= t_output, t_output starting at t0 - dt0/3 (dt0: the first CFL step)
+        and advancing by dtout per file, until the first t >= tend.  Between
+        files the steps run on the device without host synchronisation; as in
+        the reference, at most one file is written per step.  Returns the
+        written paths."""
+        return run_with_output(self, tend, dtout, outdir, batch)
+
     @property
     def launches_per_step(self) -> int:
         return int(self.lib.omhd_solver_launches_per_step(self._h))
+
+
+def run_with_output(solver, tend: float, dtout: float, outdir: str = "data", batch: int = 64) -> list:
+    """Output cadence of the reference's main loop (2D_basic/main.f90:41-75) over
+    a solver's sync / set_tend / step / run_until / write_snapshot calls.
+
+    The reference writes, at the top of each loop iteration, one file if
+    t >= t_output (then t_output += dtout), stops if t >= tend, and otherwise
+    takes one step; t_output starts at -dt/3 with dt the first CFL step, and
+    a first dt above dtout stops the run (main.f90:44-47).  Here the steps
+    between two files are enqueued with the device-side end time set to the
+    next output time, so the files fall on the same steps."""
+    import os
+
+    info = solver.sync()
+    t, dt0 = info.t, info.dt
+    if dt0 > dtout:
+        raise ValueError(f"error: {dt0} > {dtout} (the first dt exceeds the output interval)")
+    os.makedirs(outdir, exist_ok=True)
+    t_output = t - dt0 / 3.0
+    n_output = 0
+    paths = []
+    while True:
+        if t >= t_output:
+            path = os.path.join(outdir, "field-%05d.dat" % n_output)
+            solver.write_snapshot(path)
+            paths.append(path)
+            n_output += 1
+            t_output += dtout
+        if t >= tend:
+            break
+        target = min(t_output, tend)
+        if t >= target:  # the next output time has already passed: one step, as the reference's loop
+            solver.set_tend(tend)
+            solver.step(1)
+            info = solver.sync()
+        else:
+            info = solver.run_until(target, batch=batch)
+        t = info.t
+    solver.set_tend(tend)
+    return paths
