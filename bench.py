@@ -343,7 +343,10 @@ def run_ours(args):
     if not args.no_sq:
         line["ot4096sq"] = _leg(run_sq4096, args, fp64_peak)
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = _leg(lambda: cpu_baseline(steps_budget_s=10.0)[0])
+        base = _leg(lambda: cpu_baseline(steps_budget_s=10.0)[0])
+        if "error" not in base:  # the same oracle on one core, beside the all-core figure
+            base["serial"] = _leg(lambda: cpu_baseline(steps_budget_s=4.0, omp=False)[0])
+        line["cpu_baseline"] = base
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
