@@ -110,3 +110,20 @@ def test_adjoint_and_noalloc_argument_checks(lib):
               dataclasses.replace(kh, bc_kind=(0, 0, 0, 1, 0, 0))):
         st = lib.omhd_step2d_noalloc(U.ctypes.data, C.byref(c.to_c()), 0.0, 1, None, C.byref(info))
         assert st == OMHD_BAD_ARG, c
+
+
+def test_routine_wrappers_check_arrays_before_any_gpu_work(lib):
+    """The reference-named Python wrappers refuse arrays that are not
+    C-contiguous float64, and shapes that are not 2D or 3D planes, before
+    anything reaches the device."""
+    import numpy as np
+
+    from openmhd_gb300 import routines
+
+    U = np.zeros((9, 6, 7))
+    with pytest.raises(TypeError):
+        routines.u2v(U.astype(np.float32), np.zeros((4, 6, 7)))
+    with pytest.raises(TypeError):
+        routines.u2v(np.asfortranarray(U), np.zeros((4, 6, 7)))
+    with pytest.raises(ValueError):
+        routines.u2v(np.zeros((9, 7)), np.zeros((4, 7)))
