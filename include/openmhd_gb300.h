@@ -200,6 +200,12 @@ void omhd_release_host_mirrors(void);
 /* measured FP64 FMA throughput of the current GPU in GFLOP/s (roofline denominator;
  * no counterpart in the reference) */
 int omhd_probe_fp64_peak(double* gflops);
+/* accuracy probe of the fast FP64 arithmetic of the performance kernels (no
+ * counterpart in the reference): for n device doubles x, writes 5*n device
+ * doubles to out, planes rcp_nr(x), 1.0/x, rsqrt_nr(x), sqrt_nr(x), sqrt(x)
+ * (the second and last by the device's IEEE division and square root);
+ * synchronous, on the default stream */
+int omhd_probe_fastmath(const double* x_dev, long long n, double* out_dev);
 
 /* ======================================================================
  * Fused solver handle
@@ -324,10 +330,14 @@ int omhd_ensemble_sync(omhd_ensemble* e, omhd_step_info* infos);
  * loading the library holds until exit; grids needing more scratch than that
  * (9*ix*jx + ix + jx + 64 doubles, about 419k cells) are rejected with
  * OMHD_BAD_ARG and a message in omhd_last_error().  U must be device memory
- * (ix*jx*9 doubles, reference layout); bc is applied to it, then nsteps
- * steps run from time t0 on `stream` and the call waits for them.  Every call
- * reuses the same array: calls that overlap on the GPU race.  The first call
- * on a device (with it current) looks up the array's device address, so it
+ * of the current device (ix*jx*9 doubles, reference layout; memory of another
+ * device is refused with OMHD_BAD_ARG); bc is applied to it, then nsteps
+ * steps run from time t0 on `stream`.  The call is synchronous: it reads the
+ * step record back and waits for the stream before it returns, and a failure
+ * the kernels record (negative pressure or density, dt too small) is returned
+ * with its cell and value in omhd_last_error().  Every call reuses the same
+ * array: calls that overlap on the GPU race.  The first call on a device
+ * (with it current) looks up the array's device address and SM count, so it
  * should come before any stream capture.
  * ==================================================================== */
 int omhd_step2d_noalloc(double* U_dev, const omhd_config* cfg, double t0, int nsteps, void* stream,

@@ -22,13 +22,16 @@ namespace omhd {
 //   sqrt_nr  : the same series applied to s0 = x*r0 ~ sqrt(x):
 //              sqrt(x) = s0*(1-e)^(-1/2) with e = 1 - s0*r0, 5 FP64
 //              operations.
-// Each returns the double nearest the true value to within ~1 ulp (maximum
-// relative error 2.2e-16 over 2^-60..2^59, measured; two Newton-Raphson steps,
-// the textbook alternative, cost 4 and 8 operations).  The seeds flush
+// Each returns a double within 1 ulp of the correctly rounded value (two
+// Newton-Raphson steps, the textbook alternative, cost 4 and 8 operations);
+// tests/test_gpu_fastmath.py enforces the 1-ulp bound on the GPU over
+// 2^-60..2^59 and over each function's whole domain.  The seeds flush
 // subnormal arguments, so rsqrt_nr and sqrt_nr take the IEEE operation outside
 // the positive normal range (a branch that the solver's positive normal
-// arguments never take).  The parity variant (FAST = false) keeps the
-// reference's IEEE operations.
+// arguments never take); rcp_nr has no such branch and is meant for
+// |x| in [2^-1022, 2^1022] (x and 1/x normal); the solver's denominators
+// (densities, wave-speed differences, star-state factors) lie far inside it.  The parity variant (FAST = false) keeps the reference's
+// IEEE operations.
 // ---------------------------------------------------------------------------
 #ifdef __CUDACC__
 __device__ __forceinline__ double rcp_nr(double x) {

@@ -41,6 +41,7 @@ constexpr size_t kTPB = 256;
 
 constexpr int kMaxDevices = 64;
 double* g_scratch_ptr[kMaxDevices] = {nullptr};
+int g_sm_count[kMaxDevices] = {0};
 
 inline size_t align32(size_t n) { return (n + 31) & ~size_t(31); }
 
@@ -105,7 +106,7 @@ __global__ void k_na_coords(double* x, int ix, double x0, double dx, double* y, 
 // Once per device, with that device current: the device address of the
 // static scratch array (a host-side reference to the symbol is not a device
 // address and must never be handed to a kernel).
-int scratch_address(double** out) {
+int scratch_address(double** out, int* sms) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
     cudaGetLastError();
@@ -122,9 +123,17 @@ int scratch_address(double** out) {
       set_host_error(OMHD_CUDA_ERR, 0, 0, 0, 0.0, msg);
       return OMHD_CUDA_ERR;
     }
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+      cudaGetLastError();
+      set_host_error(OMHD_CUDA_ERR, 0, 0, 0, 0.0, "no-alloc step: cannot read the device's SM count");
+      return OMHD_CUDA_ERR;
+    }
+    g_sm_count[dev] = n;
     g_scratch_ptr[dev] = static_cast<double*>(p);
   }
   *out = g_scratch_ptr[dev];
+  *sms = g_sm_count[dev];
   return OMHD_OK;
 }
 
@@ -139,7 +148,10 @@ size_t omhd_step2d_noalloc_max_doubles(void) { return OMHD_NOALLOC_SCRATCH_DOUBL
 
 int omhd_step2d_noalloc(double* U, const omhd_config* cfg, double t0, int nsteps, void* stream,
                         omhd_step_info* info) {
-  if (!U || !cfg || nsteps < 0) return OMHD_BAD_ARG;
+  if (!U || !cfg || nsteps < 0) {
+    set_host_error(OMHD_BAD_ARG, 0, 0, 0, 0.0, "no-alloc step: U and cfg are required and nsteps must be >= 0");
+    return OMHD_BAD_ARG;
+  }
   if (cfg->nd != 2 || cfg->kx != 1 || cfg->ix < 4 || cfg->jx < 4 || !(cfg->dx > 0) || !(cfg->dy > 0) ||
       cfg->precision < 0 || cfg->precision > 2 || cfg->flux_type < 0 || cfg->flux_type > 4 || cfg->lm_type < 0 ||
       cfg->lm_type > 4 || (cfg->time_type != 0 && cfg->time_type != 1) || cfg->eta_kind < 0 || cfg->eta_kind > 2) {
@@ -152,7 +164,11 @@ int omhd_step2d_noalloc(double* U, const omhd_config* cfg, double t0, int nsteps
     return OMHD_BAD_ARG;
   }
   const bool iso = cfg->dx == cfg->dy;
-  if (cfg->eta_kind != OMHD_ETA_NONE && !iso) return OMHD_NOT_SUPPORTED;
+  if (cfg->eta_kind != OMHD_ETA_NONE && !iso) {
+    set_host_error(OMHD_NOT_SUPPORTED, 0, 0, 0, 0.0,
+                   "no-alloc step: resistive terms need equal grid spacings (dx == dy)");
+    return OMHD_NOT_SUPPORTED;
+  }
   const size_t n = (size_t)cfg->ix * cfg->jx;
   const size_t u1_off = align32(kCoordOff + (size_t)cfg->ix + (size_t)cfg->jx);
   const size_t need = u1_off + (size_t)NV * n;
@@ -173,8 +189,23 @@ int omhd_step2d_noalloc(double* U, const omhd_config* cfg, double t0, int nsteps
     set_host_error(OMHD_BAD_ARG, 0, 0, 0, 0.0, "no-alloc step: U must be device memory");
     return OMHD_BAD_ARG;
   }
+  int cur = -1;
+  if (cudaGetDevice(&cur) != cudaSuccess) {
+    cudaGetLastError();
+    set_host_error(OMHD_CUDA_ERR, 0, 0, 0, 0.0, "no-alloc step: no usable current CUDA device");
+    return OMHD_CUDA_ERR;
+  }
+  if (attr.type == cudaMemoryTypeDevice && attr.device != cur) {
+    // the scratch array and the kernels belong to the current device
+    char msg[160];
+    snprintf(msg, sizeof msg, "no-alloc step: U is memory of device %d, but device %d is current", attr.device,
+             cur);
+    set_host_error(OMHD_BAD_ARG, 0, 0, 0, 0.0, msg);
+    return OMHD_BAD_ARG;
+  }
   double* base = nullptr;
-  int r = scratch_address(&base);
+  int sms = 0;
+  int r = scratch_address(&base, &sms);
   if (r) return r;
   cudaStream_t s = (cudaStream_t)stream;
   StepState* st = reinterpret_cast<StepState*>(base + kRecordOff);
@@ -212,7 +243,7 @@ int omhd_step2d_noalloc(double* U, const omhd_config* cfg, double t0, int nsteps
   StepConsts sc{cfg->cfl, dmin, cfg->dx, cfg->eta_kind};
   const long long cells = (long long)(cfg->ix - 2) * (cfg->jx - 2);
   int blocks = ceil_div(cells, kTPB);
-  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks > sms * 8) blocks = sms * 8;
   k_na_plan<<<blocks, kTPB, 0, s>>>(U, cfg->ix, cfg->jx, cfg->gamma, st, err, sc);
   r = cuda_status(cudaGetLastError(), "no-alloc planning kernel");
   if (r) return r;
@@ -274,6 +305,19 @@ int omhd_step2d_noalloc(double* U, const omhd_config* cfg, double t0, int nsteps
     info->steps = out.steps;
     info->done = out.done;
     info->status = de.code;
+  }
+  if (de.code != 0) {
+    // the device's failure record, with the 1-based cell, for omhd_last_error()
+    char msg[200];
+    if (de.code == OMHD_NEG_PRESSURE)
+      snprintf(msg, sizeof msg, "negative pressure at %d %d P: %.17g", de.i, de.j, de.value);
+    else if (de.code == OMHD_NEG_DENSITY)
+      snprintf(msg, sizeof msg, "negative density at %d %d rho: %.17g", de.i, de.j, de.value);
+    else if (de.code == OMHD_DT_TOO_SMALL)
+      snprintf(msg, sizeof msg, " dt is too small : %.17g < 1e-07", de.value);
+    else
+      snprintf(msg, sizeof msg, "no-alloc step: device error %d", de.code);
+    set_host_error(de.code, de.i, de.j, de.k, de.value, msg);
   }
   return de.code;
 }

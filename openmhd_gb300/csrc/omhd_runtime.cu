@@ -5,6 +5,7 @@
 #include <mutex>
 
 #include "omhd_common.cuh"
+#include "omhd_fastmath.h"
 #include "omhd_runtime.h"
 
 namespace omhd {
@@ -151,11 +152,43 @@ __global__ void k_dfma_probe(double* out, double seed, int iters, int flag) {
   if (flag) out[blockIdx.x * blockDim.x + threadIdx.x] = sum;
 }
 
+// The fast FP64 reciprocal, reciprocal square root and square root of the
+// performance kernels beside the device's IEEE division and square root, for
+// accuracy tests: out holds five planes of n values each,
+// rcp_nr(x), 1.0/x, rsqrt_nr(x), sqrt_nr(x), sqrt(x).
+__global__ void k_fastmath_probe(const double* __restrict__ x, long long n, double* __restrict__ out) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    out[i] = rcp_nr(v);
+    out[n + i] = 1.0 / v;
+    out[2 * n + i] = rsqrt_nr(v);
+    out[3 * n + i] = sqrt_nr(v);
+    out[4 * n + i] = sqrt(v);
+  }
+}
+
 }  // namespace omhd
 
 using namespace omhd;
 
 extern "C" {
+
+int omhd_probe_fastmath(const double* x, long long n, double* out) {
+  if (!x || !out || n < 0) return OMHD_BAD_ARG;
+  if (n == 0) return OMHD_OK;
+  cudaPointerAttributes ax, ao;
+  if (cudaPointerGetAttributes(&ax, x) != cudaSuccess || cudaPointerGetAttributes(&ao, out) != cudaSuccess ||
+      ax.type != cudaMemoryTypeDevice || ao.type != cudaMemoryTypeDevice) {
+    cudaGetLastError();
+    set_host_error(OMHD_BAD_ARG, 0, 0, 0, 0.0, "fast-math probe: x and out must be device memory");
+    return OMHD_BAD_ARG;
+  }
+  long long blocks = (n + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  k_fastmath_probe<<<(unsigned)blocks, 256>>>(x, n, out);
+  if (cuda_status(cudaGetLastError(), "fast-math probe launch")) return OMHD_CUDA_ERR;
+  return cuda_status(cudaDeviceSynchronize(), "fast-math probe");
+}
 
 int omhd_probe_fp64_peak(double* gflops) {
   if (!gflops) return OMHD_BAD_ARG;

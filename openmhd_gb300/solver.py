@@ -367,31 +367,51 @@ class Solver:
                 raise OmhdError(OMHD_TIMEOUT, "run_until made no progress")
             last = info.steps
 
-    def run_with_output(self, tend: float, dtout: float, outdir: str = "data", batch: int = 64) -> list:
+    def run_with_output(self, tend: float, dtout: float, outdir: str = "data", batch: int = 64,
+                        n_start: int = 0) -> list:
         """The reference driver's time loop with snapshot output (2D_basic/main.f90:36-75):
         a field file `outdir/field-NNNNN.dat` at the start and then at the first
         t >= t_output, t_output starting at t0 - dt0/3 (dt0: the first CFL step)
         and advancing by dtout per file, until the first t >= tend.  Between
         files the steps run on the device without host synchronisation; as in
-        the reference, at most one file is written per step.  Returns the
-        written paths."""
-        return run_with_output(self, tend, dtout, outdir, batch)
+        the reference, at most one file is written per step.  `n_start` restarts
+        as the reference's MPI driver does (2D_basic/mainp.f90:85-118): n_start > 0
+        reads file n_start and continues with file n_start + 1 at t + dtout;
+        n_start < 0 first looks for the newest file from floor(tend/dtout) down.
+        Returns the written paths."""
+        return run_with_output(self, tend, dtout, outdir, batch, n_start)
 
     @property
     def launches_per_step(self) -> int:
         return int(self.lib.omhd_solver_launches_per_step(self._h))
 
 
-def run_with_output(solver, tend: float, dtout: float, outdir: str = "data", batch: int = 64) -> list:
+def snapshot_path(outdir: str, n: int) -> str:
+    """File name of snapshot n (the reference's 'data/field-',i5.5,'.dat' format, mainp.f90:277)."""
+    import os
+
+    return os.path.join(outdir, "field-%05d.dat" % n)
+
+
+def run_with_output(solver, tend: float, dtout: float, outdir: str = "data", batch: int = 64,
+                    n_start: int = 0) -> list:
     """Output cadence of the reference's main loop (2D_basic/main.f90:41-75) over
-    a solver's sync / set_tend / step / run_until / write_snapshot calls.
+    a solver's sync / set_tend / step / run_until / write_snapshot /
+    read_snapshot calls.
 
     The reference writes, at the top of each loop iteration, one file if
     t >= t_output (then t_output += dtout), stops if t >= tend, and otherwise
     takes one step; t_output starts at -dt/3 with dt the first CFL step, and
     a first dt above dtout stops the run (main.f90:44-47).  Here the steps
     between two files are enqueued with the device-side end time set to the
-    next output time, so the files fall on the same steps."""
+    next output time, so the files fall on the same steps.
+
+    Restart (2D_basic/mainp.f90:85-118): with n_start < 0 the newest existing
+    file is searched from k = floor(tend/dtout) down to 0 (n_start = 0, a
+    fresh start, if there is none); with n_start > 0 file n_start is read (its
+    t becomes the solver's time), the next file is n_start + 1 and the next
+    output time t + dtout, so the restart file itself is not written again."""
+    import math
     import os
 
     info = solver.sync()
@@ -399,12 +419,24 @@ def run_with_output(solver, tend: float, dtout: float, outdir: str = "data", bat
     if dt0 > dtout:
         raise ValueError(f"error: {dt0} > {dtout} (the first dt exceeds the output interval)")
     os.makedirs(outdir, exist_ok=True)
-    t_output = t - dt0 / 3.0
-    n_output = 0
+    if n_start < 0:
+        n_start = 0
+        for k in range(math.floor(tend / dtout), -1, -1):
+            if os.path.isfile(snapshot_path(outdir, k)):
+                n_start = k
+                break
+    if n_start == 0:
+        t_output = t - dt0 / 3.0
+        n_output = 0
+    else:
+        solver.read_snapshot(snapshot_path(outdir, n_start))
+        t = solver.sync().t
+        n_output = n_start + 1
+        t_output = t + dtout
     paths = []
     while True:
         if t >= t_output:
-            path = os.path.join(outdir, "field-%05d.dat" % n_output)
+            path = snapshot_path(outdir, n_output)
             solver.write_snapshot(path)
             paths.append(path)
             n_output += 1

@@ -9,7 +9,7 @@ returned together with the SHA-256 of each file in
 tests/golden/fileio_reference_reader.npz.  tests/test_fileio.py writes the same
 states again and checks the file bytes and our reader against that record.
 
-    python tests/golden/make_fileio_golden.py [reference checkout, default /root/reference]
+    python tests/golden/make_fileio_golden.py <path of the OpenMHD checkout>
 """
 from __future__ import annotations
 
@@ -86,4 +86,6 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_fileio_golden.py <path of the OpenMHD checkout>")
+    main(sys.argv[1])

@@ -110,6 +110,18 @@ def test_adjoint_and_noalloc_argument_checks(lib):
               dataclasses.replace(kh, bc_kind=(0, 0, 0, 1, 0, 0))):
         st = lib.omhd_step2d_noalloc(U.ctypes.data, C.byref(c.to_c()), 0.0, 1, None, C.byref(info))
         assert st == OMHD_BAD_ARG, c
+    # every refusal of the no-alloc step leaves a message for omhd_last_error()
+    from openmhd_gb300 import reconnection2d
+
+    rc, _ = reconnection2d(32, 16)
+    for c, code, words in ((dataclasses.replace(rc, dy=2 * rc.dx), OMHD_NOT_SUPPORTED, b"equal grid spacings"),
+                           (kh, OMHD_BAD_ARG, b"required")):
+        lib.omhd_clear_error()
+        st = lib.omhd_step2d_noalloc(None if code == OMHD_BAD_ARG else U.ctypes.data, C.byref(c.to_c()), 0.0, 1,
+                                     None, C.byref(info))
+        e = _lib.ErrorInfo()
+        assert st == code and lib.omhd_last_error(C.byref(e)) == code and words in e.message, (st, e.message)
+    lib.omhd_clear_error()
 
 
 def test_routine_wrappers_check_arrays_before_any_gpu_work(lib):
@@ -127,3 +139,39 @@ def test_routine_wrappers_check_arrays_before_any_gpu_work(lib):
         routines.u2v(np.asfortranarray(U), np.zeros((4, 6, 7)))
     with pytest.raises(ValueError):
         routines.u2v(np.zeros((9, 7)), np.zeros((4, 7)))
+
+
+def test_routine_wrappers_refuse_undersized_arrays(lib):
+    """Every array a wrapper hands to the library must have the shape the
+    routine reads or writes, derived from U (or F, wk, VL): an undersized V, F,
+    face-state array or coordinate vector is refused before any library call,
+    instead of being overrun by a copy or a kernel."""
+    import numpy as np
+
+    from openmhd_gb300 import routines
+
+    U = np.zeros((9, 6, 7))
+    with pytest.raises(ValueError, match="V has shape"):
+        routines.u2v(U, np.zeros((4, 6, 6)))
+    with pytest.raises(ValueError, match="V has shape"):
+        routines.set_dt(U, np.zeros((3, 6, 7)), 0.1, 0.4)
+    with pytest.raises(ValueError, match="wR has shape"):
+        routines.limiter(np.zeros((6, 7)), np.zeros((6, 7)), np.zeros((6, 6)), 1, 1)
+    with pytest.raises(ValueError, match="VR has shape"):
+        routines.flux_solver(np.zeros((9, 6, 7)), np.zeros((9, 6, 7)), np.zeros((9, 5, 7)), 1.0, 1, 3)
+    with pytest.raises(ValueError, match="G has shape"):
+        routines.rk_tvd21(U, np.zeros_like(U), np.zeros_like(U), np.zeros((9, 6, 6)), dt=0.1, dx=0.1)
+    with pytest.raises(ValueError, match="H is required"):
+        routines.rk_tvd22(np.zeros((9, 4, 6, 7)), np.zeros((9, 4, 6, 7)), np.zeros((9, 4, 6, 7)),
+                          np.zeros((9, 4, 6, 7)), dt=0.1, dx=0.1)
+    with pytest.raises(ValueError, match="F has shape"):
+        routines.flux_resistive(np.zeros((9, 6, 6)), U, np.zeros(7), np.zeros(6), dx=0.1, dir=1)
+    with pytest.raises(ValueError, match="x has shape"):
+        routines.flux_resistive(np.zeros_like(U), U, np.zeros(6), np.zeros(6), dx=0.1, dir=1)
+    with pytest.raises(ValueError, match="z has shape"):
+        U3 = np.zeros((9, 4, 6, 7))
+        routines.flux_resistive(np.zeros_like(U3), U3, np.zeros(7), np.zeros(6), np.zeros(3), dx=0.1, dir=1)
+    with pytest.raises(ValueError, match="VR has shape"):
+        routines.facefix(np.zeros((9, 6, 7)), np.zeros((9, 6, 8)), 1)
+    with pytest.raises(ValueError, match="one entry per domain side"):
+        routines.bc(U, kind=(0, 0, 0, 0))

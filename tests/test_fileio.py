@@ -112,6 +112,31 @@ def test_solver_snapshot_and_restart(cuda_lib, tmp_path, oracle_mod):
     assert np.array_equal(a.get_state_numpy(), b.get_state_numpy())
 
 
+@pytest.mark.gpu
+def test_run_with_output_restart_from_newest_file(cuda_lib, tmp_path):
+    """The driver-level restart (2D_basic/mainp.f90:85-118) on the GPU solver:
+    a run to t = 0.3 with output every 0.1, then a fresh solver with
+    n_start = -1 finds the newest file, continues with the next file number
+    and ends on the state an uninterrupted run reaches, bit for bit (the
+    output times only set where the device stops between files, never dt)."""
+    import os
+
+    from openmhd_gb300 import Solver, orszag_tang
+
+    cfg, model = orszag_tang(48)
+    out = str(tmp_path / "data")
+    first = Solver(cfg).init_model(model).run_with_output(0.3, 0.1, outdir=out)
+    assert [os.path.basename(p) for p in first] == ["field-%05d.dat" % n for n in range(4)]
+    b = Solver(cfg).init_model(model)
+    second = b.run_with_output(0.6, 0.1, outdir=out, n_start=-1)
+    assert os.path.basename(second[0]) == "field-00004.dat"
+    whole = Solver(cfg).init_model(model)
+    whole.run_until(0.6)
+    ib, iw = b.sync(), whole.sync()
+    assert ib.t == iw.t and ib.t >= 0.6
+    assert np.array_equal(b.get_state_numpy(), whole.get_state_numpy())
+
+
 def test_layout_pinned_by_reference_readers(lib, tmp_path):
     """The files written for the seeded states of tests/golden/make_fileio_golden.py
     are byte for byte the files that the reference's own readers

@@ -65,3 +65,35 @@ def test_autotune_leaves_state_unchanged(cuda_lib):
     for i in range(len(cfgs)):
         assert np.array_equal(ens.member_state(i), before[i])
         assert info1[i].steps == info0[i].steps and info1[i].t == info0[i].t
+
+
+def test_members_at_bench_sizes_vs_oracle(cuda_lib, oracle_mod):
+    """FP64 ensemble members at the batched configuration's side lengths
+    (256..1024, one Orszag-Tang and one Kelvin-Helmholtz member, non-square)
+    against the oracle directly, from the members' own initial states: 1 step
+    within 1e-12 and 5 steps within 1e-9 per variable (scaled L1 and own-norm
+    relative L1 above round-off), the FP64 tolerances of the single-grid path."""
+    from helpers import assert_parity
+    from openmhd_gb300.ensemble import Ensemble, batched_problem_set
+    from oracle.oracle import Grid
+
+    cfgs, models = batched_problem_set(2, seed=11, precision="fp64", sides=[256, 320, 512, 1024])
+    assert all(min(c.ix, c.jx) - 2 >= 256 for c in cfgs)
+    ens = Ensemble(cfgs).init_models(models)
+    grids = []
+    for i, c in enumerate(cfgs):
+        g = Grid.from_solver_config(c, omp=True)
+        g.U[...] = ens.member_state(i)
+        grids.append(g)
+    ens.step(1)
+    infos = ens.sync()
+    for i, g in enumerate(grids):
+        g.step(1)
+        assert infos[i].status == 0 and abs(infos[i].dt - g.last_dt) <= 1e-14 * g.last_dt
+        assert_parity(ens.member_state(i), g.U, 1e-12, f"member {i}, 1 step")
+    ens.step(4)
+    infos = ens.sync()
+    for i, g in enumerate(grids):
+        g.step(4)
+        assert infos[i].steps == 5
+        assert_parity(ens.member_state(i), g.U, 1e-9, f"member {i}, 5 steps")

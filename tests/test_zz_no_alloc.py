@@ -95,3 +95,31 @@ def test_noalloc_rejects_grid_beyond_fixed_scratch(cuda_lib):
     lib.omhd_last_error(C.byref(e))
     assert b"scratch" in e.message
     lib.omhd_clear_error()
+
+
+def test_noalloc_reports_device_failure_with_cell(cuda_lib):
+    """A failure the stage kernels record (here negative pressure) comes back
+    from the call as its status and through omhd_last_error() with the
+    1-based cell and the value, as the solver's sync reports it."""
+    import torch
+
+    from openmhd_gb300 import Solver, _lib, orszag_tang
+
+    lib = cuda_lib
+    cfg, model = orszag_tang(32)
+    U0 = Solver(cfg).init_model(model).get_state_numpy()
+    U0[3, 10, 12] = -5.0  # E < 0 at Fortran (13, 11)
+    U = torch.from_numpy(U0).cuda()
+    cfg_c = cfg.to_c()
+    lib.omhd_clear_error()
+    info = _lib.StepInfo()
+    st = lib.omhd_step2d_noalloc(U.data_ptr(), C.byref(cfg_c), 0.0, 2, None, C.byref(info))
+    e = _lib.ErrorInfo()
+    assert st == 1 and info.status == 1 and info.steps == 0
+    assert lib.omhd_last_error(C.byref(e)) == 1 and (e.i, e.j) == (13, 11), (e.i, e.j, e.message)
+    assert b"negative pressure at 13 11" in e.message
+    lib.omhd_clear_error()
+    # the next call on the shared scratch starts clean
+    U1 = torch.from_numpy(Solver(cfg).init_model(model).get_state_numpy()).cuda()
+    st = lib.omhd_step2d_noalloc(U1.data_ptr(), C.byref(cfg_c), 0.0, 2, None, C.byref(info))
+    assert st == 0 and info.status == 0 and info.steps == 2
