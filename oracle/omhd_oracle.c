@@ -3,8 +3,8 @@
  *
  * TEST INFRASTRUCTURE ONLY (the oracle).  The product never links or calls
  * this file; tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs
- * do.  Parity status: UNPINNED (the reference ships no golden vectors and no
- * Fortran compiler is available to run it); see omhd_oracle.h.
+ * do.  Parity status: PINNED to the reference's own source, executed through
+ * its mechanical C translation (oracle/ref.py); see omhd_oracle.h.
  *
  * Every routine restates one reference routine in the reference's own
  * operation order.  Fortran semantics kept on purpose:

@@ -5,13 +5,20 @@
  * loads or calls this code; only tests/, __graft_entry__.smoke() and the
  * CPU-baseline legs of bench.py use it, to check results against.
  *
- * Parity status: UNPINNED.  The reference (zenitani/OpenMHD) is Fortran 90,
+ * Parity status: PINNED.  The reference (zenitani/OpenMHD) is Fortran 90 and
  * ships no tests, fixtures or golden vectors, and no Fortran compiler exists
- * where this project is built, so the restatement cannot be diffed against the
- * reference's own outputs.  It follows the reference routine by routine, in
- * the reference's operation order (every function cites the file:line it
- * restates), and is compiled with -ffp-contract=off so that each Fortran
- * expression maps to the same sequence of IEEE-754 double operations.
+ * where this project is built.  oracle/ref.py therefore translates the
+ * reference's own source files (the routines, model.f90 and main.f90 of
+ * 2D_basic, 2D_KH, 2D_reconnection and 3D_basic) mechanically into C
+ * (oracle/f90sub.py) and builds them into oracle/_ref/; tests/
+ * test_ref_translation.py runs those reference drivers and routines and
+ * requires this restatement to give the same bits (every limiter, flux and
+ * time integrator, the HLLD branches, walls, resistivity, 2D and 3D), and
+ * tests/test_ref_golden.py checks it against fixtures recorded from them.
+ * This file follows the reference routine by routine, in the reference's
+ * operation order (every function cites the file:line it restates), and is
+ * compiled with -ffp-contract=off so that each Fortran expression maps to the
+ * same sequence of IEEE-754 double operations.
  *
  * Array layout is the reference's: Fortran column-major U(ix,jx[,kx],var) with
  * i fastest and the variable index slowest.  2D arrays are 3D arrays with

@@ -2,8 +2,9 @@
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
 CPU-baseline legs of bench.py, to check results against.  The product (openmhd_gb300/)
-never imports it.  Parity status: unpinned (no reference golden vectors exist
-and no Fortran compiler is available to run the reference itself).
+never imports it.  Parity status: pinned to the reference's own source, which
+oracle/ref.py executes through a mechanical C translation (no Fortran compiler
+is available): tests/test_ref_translation.py and tests/test_ref_golden.py.
 
 State arrays are numpy float64 arrays shaped (9, jx, ix) or (9, kx, jx, ix):
 the same memory as the reference's column-major U(ix,jx[,kx],var).
