@@ -47,6 +47,85 @@ def _load_flops(name: str = "flops_kh2d.txt"):
     return 2100.0  # estimate until the counting build has run
 
 
+def _load_flops_split(name: str):
+    """(total, face-flux part, rest) flops per cell-update from a profiles/ flop
+    count: the face part (limiters, face fixes, Riemann solver, resistive face
+    terms) is what the FP32-mixed kernels compute in FP32, the rest (u2v, CFL,
+    GLM, RK update) their FP64 residual."""
+    p = os.path.join(ROOT, "profiles", name)
+    txt = open(p).read()
+    get = lambda k: float(re.search(k + r":\s*([0-9.]+)", txt).group(1))  # noqa: E731
+    return get("flops_per_cell_update"), get("face_flux_flops_per_cell_update"), get("rest_flops_per_cell_update")
+
+
+def _mixed_roofline(cells_per_s: float, split, fp64_peak_gflops: float, fp32_peak_gflops: float,
+                    hbm_peak_gbs: float, bytes_per_cu: float = BYTES_PER_CELL_UPDATE_2D):
+    """Roofline of an FP32-mixed run: the time per cell-update is bounded by
+    the slowest of its FP64 residual flops at the FP64 peak, its FP32 face-flux
+    flops at the FP32 peak and its bytes at the HBM peak.  `achieved`/`frac`
+    are those of the binding resource (the FP64 residual on GB300, whose FP64
+    pipe is 1/64 of its FP32 rate); `roof_frac` = roof time / measured time."""
+    _, face, rest = split
+    t64 = rest / (fp64_peak_gflops * 1e9)
+    t32 = face / (fp32_peak_gflops * 1e9)
+    tb = bytes_per_cu / (hbm_peak_gbs * 1e9)
+    parts = {"fp64": (rest, fp64_peak_gflops / 1e3, t64, "TFLOP/s"), "fp32": (face, fp32_peak_gflops / 1e3, t32,
+                                                                               "TFLOP/s"),
+             "hbm": (bytes_per_cu, hbm_peak_gbs, tb, "GB/s")}
+    bound = max(parts, key=lambda k: parts[k][2])
+    out = {"bound": bound}
+    for k, (per_cu, peak, troof, unit) in parts.items():
+        ach = per_cu * cells_per_s / (1e12 if unit == "TFLOP/s" else 1e9)
+        out[k] = {"per_cell_update": per_cu, "achieved": ach, "peak": peak, "unit": unit, "frac": ach / peak}
+    out["achieved"], out["peak"], out["unit"], out["frac"] = (out[bound]["achieved"], out[bound]["peak"],
+                                                              out[bound]["unit"], out[bound]["frac"])
+    out["roof_frac"] = max(t64, t32, tb) * cells_per_s
+    return out
+
+
+def _fp64_roofline(cells_per_s: float, flops_cu: float, fp64_peak_gflops: float, hbm_peak_gbs: float,
+                   bytes_per_cu: float = BYTES_PER_CELL_UPDATE_2D):
+    ach = flops_cu * cells_per_s / 1e12
+    hbm = bytes_per_cu * cells_per_s / 1e9
+    return {"bound": "fp64", "achieved": ach, "peak": fp64_peak_gflops / 1e3, "unit": "TFLOP/s",
+            "frac": ach / (fp64_peak_gflops / 1e3), "flops_per_cell_update": flops_cu,
+            "hbm": {"achieved": hbm, "peak": hbm_peak_gbs, "unit": "GB/s", "frac": hbm / hbm_peak_gbs}}
+
+
+def _errors(a, b):
+    """Per-variable error of state a against b ((9, ...) numpy arrays or torch
+    tensors; tensors are reduced on their device): scaled L1
+    (openmhd_gb300.metrics.scaled_l1), relative L1 against each variable's own
+    norm, and the max norm; plus the largest own-norm error over the variables
+    that hold at least 1e-4 of their physical scale."""
+    import numpy as np
+    import torch
+
+    from openmhd_gb300.metrics import VAR_NAMES
+
+    if isinstance(a, np.ndarray):
+        a, b = torch.from_numpy(np.ascontiguousarray(a)), torch.from_numpy(np.ascontiguousarray(b))
+    a = a.reshape(9, -1)
+    b = b.reshape(9, -1)
+    num = torch.stack([(a[v] - b[v]).abs().sum() for v in range(9)])
+    li = torch.stack([(a[v] - b[v]).abs().max() for v in range(9)])
+    norm = torch.stack([b[v].abs().sum() for v in range(9)])
+    m = torch.sqrt((2.0 * b[4] * b[3]).abs()).sum()
+    B = torch.sqrt(b[5] * b[5] + b[6] * b[6] + b[7] * b[7]).sum()
+    scale = torch.stack([m, m, m, norm[3], norm[4], B, B, B, B])
+    num, li, norm, scale = (x.double().cpu().numpy() for x in (num, li, norm, scale))
+    floor = max(scale.max(), 1e-300) * 1e-12
+    sc = num / np.maximum(scale, floor)
+    own = np.where(norm > 0, num / np.where(norm > 0, norm, 1.0), num)
+    sig = norm >= 1e-4 * scale
+    return {"scaled_l1": dict(zip(VAR_NAMES, map(float, sc))),
+            "own_norm_rel_l1": dict(zip(VAR_NAMES, map(float, own))),
+            "linf": dict(zip(VAR_NAMES, map(float, li))),
+            "max_scaled_l1": float(sc.max()),
+            "max_own_norm_rel_l1_significant": float(own[sig].max()) if sig.any() else 0.0,
+            "significant_vars": [v for v, g in zip(VAR_NAMES, sig) if g]}
+
+
 def _load_traffic(name: str):
     p = os.path.join(ROOT, "profiles", name)
     if os.path.exists(p):
@@ -258,11 +337,8 @@ def run_ours(args):
     e1.synchronize()
     im = m.sync()
     t_mx = e0.elapsed_time(e1) / 1e3
-    from openmhd_gb300.metrics import VAR_NAMES as names, rel_l1, scaled_l1
-
     Um = m.get_state_numpy()
-    l1 = rel_l1(Um[:, 1:-1, 1:-1], U64[:, 1:-1, 1:-1])
-    sl1 = scaled_l1(Um[:, 1:-1, 1:-1], U64[:, 1:-1, 1:-1])
+    mixed_err = _errors(Um[:, 1:-1, 1:-1], U64[:, 1:-1, 1:-1])
     del m
 
     # ---- end to end through the C ABI with host buffers ----
@@ -302,6 +378,7 @@ def run_ours(args):
     peaks, peak_src = _peaks()
     flops_cu = _load_flops()
     fp64_peak = _fp64_peak_gflops(lib)
+    fp32_peak = _fp32_peak_gflops(lib)
     launch_s = t_fp64 / (2 * args.steps)  # two stage launches per step, nothing else in the region
     ach_tflops = flops_cu * cells / 2 / launch_s / 1e12
     hbm_gbs = BYTES_PER_CELL_UPDATE_2D * cells / (t_fp64 / args.steps) / 1e9
@@ -331,16 +408,20 @@ def run_ours(args):
         "e2e": e2e,
         "clocks": clk.summary(),
         "mixed": {"value": ws * cells * args.steps / t_mx, "speedup_vs_fp64": t_fp64 / t_mx,
-                  "scaled_l1_vs_fp64": dict(zip(names, [float(x) for x in sl1])),
-                  "own_norm_rel_l1_vs_fp64": dict(zip(names, [float(x) for x in l1])), "status": im.status,
+                  "roofline": _mixed_roofline(cells * args.steps / t_mx, _load_flops_split("flops_kh2d.txt"),
+                                              fp64_peak, fp32_peak, peaks.get("hbm_gbs", 6800.0)),
+                  "error_vs_fp64": mixed_err, "status": im.status,
                   "steps_compared": args.warmup + args.steps},
+        "peaks_in_run": {"fp64_gflops": fp64_peak, "fp32_gflops": fp32_peak,
+                         "source": "omhd_probe_fp64_peak / omhd_probe_fp32_peak (FMA chains in registers, best "
+                                   "of five launches); HBM from MEASURED_PEAKS.json"},
     }
     if not args.no_batched:
-        line["batched"] = _leg(run_batched, args)
+        line["batched"] = _leg(run_batched, args, fp64_peak, fp32_peak)
     if not args.no_adjoint:
         line["adjoint"] = _leg(run_adjoint, args)
     if not args.no_3d:
-        line["harris3d"] = _leg(run_3d, args)
+        line["harris3d"] = _leg(run_3d, args, fp64_peak, fp32_peak)
     if not args.no_sq:
         line["ot4096sq"] = _leg(run_sq4096, args, fp64_peak)
     if rank == 0 and not args.no_cpu_baseline:
@@ -357,7 +438,7 @@ def run_ours(args):
     return 0
 
 
-def run_batched(args):
+def run_batched(args, fp64_peak: float = float("nan"), fp32_peak: float = float("nan")):
     """128-member ensemble (seeded sizes in {128..1024}^2, half OT, half KH),
     FP32-mixed, one persistent batched kernel per RK stage, autotuned tiling,
     K steps replayed as one CUDA graph.  Every member runs 500 steps in all;
@@ -368,7 +449,6 @@ def run_batched(args):
     import torch
 
     from openmhd_gb300.ensemble import Ensemble, batched_problem_set
-    from openmhd_gb300.metrics import scaled_l1
 
     cfgs, models = batched_problem_set(128, seed=0, precision="mixed")
     ens = Ensemble(cfgs).init_models(models)
@@ -408,13 +488,23 @@ def run_batched(args):
     updates64 = sum(n * (a.steps - b.steps) for n, a, b in zip(cells_m, ref.sync(), before64))
     ref.step(total_steps - 3 - args.steps)
     ref.sync()
-    errs = []
+    errs, owns, lis = [], [], []
     for i in range(len(cfgs)):
-        a = ens.member_state(i)[:, 1:-1, 1:-1]
-        b = ref.member_state(i)[:, 1:-1, 1:-1]
-        errs.append(float(np.max(scaled_l1(a, b))))
+        e = _errors(ens.member_state(i)[:, 1:-1, 1:-1], ref.member_state(i)[:, 1:-1, 1:-1])
+        errs.append(e["max_scaled_l1"])
+        owns.append(e["max_own_norm_rel_l1_significant"])
+        lis.append(max(e["linf"].values()))
     del ref
+    peaks, _ = _peaks()
+    split = _load_flops_split("flops_ensemble2d.txt")
     return {"value": updates / t, "unit": "cell-updates/s", "members": len(cfgs),
+            "roofline": _mixed_roofline(updates / t, split, fp64_peak, fp32_peak, peaks.get("hbm_gbs", 6800.0)),
+            "fp64_roofline": _fp64_roofline(updates64 / t64, split[0], fp64_peak, peaks.get("hbm_gbs", 6800.0)),
+            "max_member_own_norm_rel_l1_vs_fp64": max(owns),
+            "median_member_own_norm_rel_l1_vs_fp64": float(np.median(owns)),
+            "members_own_norm_within_1e-6": int(sum(o <= 1e-6 for o in owns)),
+            "members_scaled_within_1e-6": int(sum(x <= 1e-6 for x in errs)),
+            "max_member_linf_vs_fp64": max(lis),
             "members_stepping_throughout": active,
             "fp64_batched_value": updates64 / t64, "speedup_vs_fp64_batched": (updates / t) / (updates64 / t64),
             "cells": ens.cells, "precision": "mixed", "tile_kind": kind, "ctas_per_sm": cps,
@@ -465,20 +555,6 @@ def run_sq4096(args, fp64_peak_gflops: float):
 H3_NX, H3_NY, H3_NZ = 512, 256, 512
 
 
-def _scaled_l1_t(a, b):
-    """scaled_l1 (openmhd_gb300.metrics) on device tensors (9, ...)."""
-    import torch
-
-    a = a.reshape(9, -1)
-    b = b.reshape(9, -1)
-    num = (a - b).abs().sum(dim=1)
-    m = torch.sqrt((2.0 * b[4] * b[3]).abs()).sum()
-    B = torch.sqrt((b[5:8] ** 2).sum(dim=0)).sum()
-    den = torch.stack([m, m, m, b[3].abs().sum(), b[4].abs().sum(), B, B, B, B])
-    floor = torch.clamp(den.max(), min=1e-300) * 1e-12
-    return (num / torch.maximum(den, floor)).cpu().tolist()
-
-
 def _div_b_max(U, dx, dy, dz=None):
     """max |div B| over the interior, centred differences (the reference's
     diagnostic form; GLM keeps it bounded rather than zero)."""
@@ -491,7 +567,7 @@ def _div_b_max(U, dx, dy, dz=None):
     return float(d.abs().max())
 
 
-def run_3d(args):
+def run_3d(args, fp64_peak: float = float("nan"), fp32_peak: float = float("nan")):
     """3D resistive Harris sheet 512 x 256 x 512 (x, y periodic, z conducting
     walls, HLLD + MC + GLM + resistive fluxes), FP64 and FP32-mixed on the
     same steps: cell-updates/s, HBM GB/s against the 360 B per cell-update of
@@ -525,13 +601,16 @@ def run_3d(args):
         out[prec] = {"value": cells * steps / t, "unit": "cell-updates/s", "ms_per_step": 1e3 * t / steps,
                      "hbm_gbs_algorithmic": gbs, "hbm_frac": gbs / peaks.get("hbm_gbs", 1.0),
                      "hbm_peak_source": peak_src, "status": info.status, "launches_per_step": 2}
+        split = _load_flops_split("flops_harris3d.txt")
         if prec == "fp64":
             out[prec]["max_div_b"] = _div_b_max(s.U, cfg.dx, cfg.dy, cfg.dz)
+            out[prec]["roofline"] = _fp64_roofline(cells * steps / t, split[0], fp64_peak, peaks.get("hbm_gbs", 6800.0))
+        else:
+            out[prec]["roofline"] = _mixed_roofline(cells * steps / t, split, fp64_peak, fp32_peak,
+                                                    peaks.get("hbm_gbs", 6800.0))
         states[prec] = s
     out["mixed"]["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
-    from openmhd_gb300.metrics import VAR_NAMES
-
-    out["mixed"]["scaled_l1_vs_fp64"] = dict(zip(VAR_NAMES, _scaled_l1_t(states["mixed"].U, states["fp64"].U)))
+    out["mixed"]["error_vs_fp64"] = _errors(states["mixed"].U[:, 1:-1, 1:-1, 1:-1], states["fp64"].U[:, 1:-1, 1:-1, 1:-1])
     out["mixed"]["steps_compared"] = warm + steps
     del states
     torch.cuda.empty_cache()
@@ -671,11 +750,67 @@ def run_adjoint(args, ndir: int = 16, eps: float = 1e-6):
     }
 
 
+def run_accuracy(args):
+    """Error of the FP32-mixed path against the FP64 path over long runs (not
+    a throughput measurement): KH 4096 x 2048 (HLLD + minmod + GLM) for
+    --accuracy-steps steps (the configuration's 2000 by default) and the
+    resistive Harris sheet 512 x 256 x 512 (HLLD + MC + GLM) for
+    --accuracy-steps-3d steps, both solvers from the same initial state; the
+    per-variable scaled L1, own-norm relative L1 and max-norm errors at a few
+    step counts along the way, computed on the device."""
+    import torch
+
+    from openmhd_gb300 import Solver, harris3d, kelvin_helmholtz
+
+    def curve(make, total, marks):
+        cfg64, model = make("fp64")
+        cfgmx, _ = make("mixed")
+        a = Solver(cfg64).init_model(model)
+        b = Solver(cfgmx).init_model(model)
+        sl = (slice(None),) + (slice(1, -1),) * (a.U.dim() - 1)
+        out, done = [], 0
+        for mk in marks:
+            if mk > total:
+                break
+            a.step(mk - done)
+            b.step(mk - done)
+            ia, ib = a.sync(), b.sync()
+            done = mk
+            if ia.status or ib.status:
+                out.append({"steps": mk, "status": [ia.status, ib.status]})
+                break
+            e = _errors(b.U[sl], a.U[sl])
+            e.update({"steps": mk, "t_fp64": ia.t, "t_mixed": ib.t})
+            out.append(e)
+        del a, b
+        torch.cuda.empty_cache()
+        return out
+
+    marks2 = sorted({10, 100, 500, 1000, args.accuracy_steps})
+    marks3 = sorted({10, 100, 300, args.accuracy_steps_3d})
+    res = {"accuracy": {
+        "kh2d_4096x2048": curve(lambda p: kelvin_helmholtz(NX, NY, precision=p), args.accuracy_steps, marks2),
+        "harris3d_512x256x512": curve(lambda p: harris3d(H3_NX, H3_NY, H3_NZ, precision=p), args.accuracy_steps_3d,
+                                      marks3),
+    }}
+    print(json.dumps(res), flush=True)
+    return 0
+
+
 def _fp64_peak_gflops(lib) -> float:
     import ctypes as C
 
     g = C.c_double()
     if lib.omhd_probe_fp64_peak(C.byref(g)) != 0:
+        return float("nan")
+    return g.value
+
+
+def _fp32_peak_gflops(lib) -> float:
+    import ctypes as C
+
+    g = C.c_double()
+    if lib.omhd_probe_fp32_peak(C.byref(g)) != 0:
         return float("nan")
     return g.value
 
@@ -762,7 +897,16 @@ def main():
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--nz", type=int, default=0)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_parity", "mixed"])
+    ap.add_argument("--accuracy", action="store_true",
+                    help="long-run error of the FP32-mixed path against FP64 (KH 2D and Harris 3D)")
+    ap.add_argument("--accuracy-steps", type=int, default=2000)
+    ap.add_argument("--accuracy-steps-3d", type=int, default=1000)
     args = ap.parse_args()
+    if args.accuracy:
+        from openmhd_gb300.build import build
+
+        build()
+        return run_accuracy(args)
     if args.profile or args.profile_adjoint or args.profile_batched:
         from openmhd_gb300.build import build
 

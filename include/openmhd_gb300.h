@@ -200,6 +200,9 @@ void omhd_release_host_mirrors(void);
 /* measured FP64 FMA throughput of the current GPU in GFLOP/s (roofline denominator;
  * no counterpart in the reference) */
 int omhd_probe_fp64_peak(double* gflops);
+/* measured FP32 FMA throughput of the current GPU in GFLOP/s (the FP32 roofline
+ * denominator of the mixed-precision kernels; no counterpart in the reference) */
+int omhd_probe_fp32_peak(double* gflops);
 /* accuracy probe of the fast FP64 arithmetic of the performance kernels (no
  * counterpart in the reference): for n device doubles x, writes 5*n device
  * doubles to out, planes rcp_nr(x), 1.0/x, rsqrt_nr(x), sqrt_nr(x), sqrt(x)

@@ -152,6 +152,24 @@ __global__ void k_dfma_probe(double* out, double seed, int iters, int flag) {
   if (flag) out[blockIdx.x * blockDim.x + threadIdx.x] = sum;
 }
 
+// FP32 FMA throughput probe, the same shape as the FP64 one: the FP32
+// roofline denominator of the mixed-precision kernels.
+__global__ void k_ffma_probe(float* out, float seed, int iters, int flag) {
+  const float b = seed * 1.0000001f + threadIdx.x * 1e-9f;
+  const float c = 0.999999f + blockIdx.x * 1e-12f;
+  float a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = 1.0f + k * 1e-3f + threadIdx.x * 1e-7f;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fmaf(a[k], b, c);
+  }
+  float sum = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) sum += a[k];
+  if (flag) out[blockIdx.x * blockDim.x + threadIdx.x] = sum;
+}
+
 // The fast FP64 reciprocal, reciprocal square root and square root of the
 // performance kernels beside the device's IEEE division and square root, for
 // accuracy tests: out holds five planes of n values each,
@@ -206,6 +224,36 @@ int omhd_probe_fp64_peak(double* gflops) {
   for (int r = 0; r < 5; ++r) {  // best of five launches (burst rate)
     cudaEventRecord(e0);
     k_dfma_probe<<<blocks, threads>>>(out, 1.0, iters, 0);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double flops = (double)blocks * threads * (double)iters * 8 * 2;
+    if (ms > 0 && flops / (ms * 1e6) > best) best = flops / (ms * 1e6);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  *gflops = best;
+  return cuda_status(cudaGetLastError(), "probe kernel");
+}
+
+int omhd_probe_fp32_peak(double* gflops) {
+  if (!gflops) return OMHD_BAD_ARG;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return OMHD_CUDA_ERR;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8, threads = 256, iters = 16384;
+  float* out = nullptr;
+  if (cuda_status(cudaMalloc(&out, sizeof(float) * blocks * threads), "probe allocation")) return OMHD_CUDA_ERR;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_ffma_probe<<<blocks, threads>>>(out, 1.0f, iters, 0);  // warm-up
+  double best = 0.0;
+  for (int r = 0; r < 5; ++r) {  // best of five launches (burst rate)
+    cudaEventRecord(e0);
+    k_ffma_probe<<<blocks, threads>>>(out, 1.0f, iters, 0);
     cudaEventRecord(e1);
     cudaEventSynchronize(e1);
     float ms = 0;

@@ -802,8 +802,15 @@ static void limit_all(const omo_cfg* c, const double* U, const double* V, double
     omo_limiter(U + us[q] * n, VL + us[q] * n, VR + us[q] * n, c->ix, c->jx, c->kx, dir, c->lm_type);
 }
 
+/* The flop-counting build (oracle/flopcount.cpp) defines this to tally the
+ * face reconstruction and flux work of a step apart from the rest. */
+#ifndef OMO_FLUX_REGION
+#define OMO_FLUX_REGION(on)
+#endif
+
 static int half_fluxes(const omo_cfg* c, const double* Ucur, double* V, double* VL, double* VR,
                        double* Fd[3], double ch, const double* x, const double* y, const double* z) {
+  OMO_FLUX_REGION(1);
   for (int dir = 1; dir <= c->nd; ++dir) {
     limit_all(c, Ucur, V, VL, VR, dir);
     omo_facefix(VL, VR, c->ix, c->jx, c->kx, dir, &c->bc);
@@ -811,6 +818,7 @@ static int half_fluxes(const omo_cfg* c, const double* Ucur, double* V, double* 
     if (c->eta_kind != OMO_ETA_NONE)
       omo_flux_resistive(Fd[dir - 1], Ucur, x, y, z, c->dx, c->ix, c->jx, c->kx, c->nd, dir, c->eta_kind);
   }
+  OMO_FLUX_REGION(0);
   return OMO_OK;
 }
 
