@@ -762,9 +762,9 @@ def run_accuracy(args):
 
     from openmhd_gb300 import Solver, harris3d, kelvin_helmholtz
 
-    def curve(make, total, marks):
-        cfg64, model = make("fp64")
-        cfgmx, _ = make("mixed")
+    def curve(make, total, marks, pair=("fp64", "mixed")):
+        cfg64, model = make(pair[0])
+        cfgmx, _ = make(pair[1])
         a = Solver(cfg64).init_model(model)
         b = Solver(cfgmx).init_model(model)
         sl = (slice(None),) + (slice(1, -1),) * (a.U.dim() - 1)
@@ -788,11 +788,20 @@ def run_accuracy(args):
 
     marks2 = sorted({10, 100, 500, 1000, args.accuracy_steps})
     marks3 = sorted({10, 100, 300, args.accuracy_steps_3d})
+    kh = lambda p: kelvin_helmholtz(NX, NY, precision=p)  # noqa: E731
+    h3 = lambda p: harris3d(H3_NX, H3_NY, H3_NZ, precision=p)  # noqa: E731
     res = {"accuracy": {
-        "kh2d_4096x2048": curve(lambda p: kelvin_helmholtz(NX, NY, precision=p), args.accuracy_steps, marks2),
-        "harris3d_512x256x512": curve(lambda p: harris3d(H3_NX, H3_NY, H3_NZ, precision=p), args.accuracy_steps_3d,
-                                      marks3),
+        "kh2d_4096x2048": curve(kh, args.accuracy_steps, marks2),
+        "harris3d_512x256x512": curve(h3, args.accuracy_steps_3d, marks3),
     }}
+    if args.accuracy_control:
+        # control: the FP64 build against the FP64 build without multiply-add
+        # contraction, i.e. how far round-off alone (1e-16 per operation) is
+        # carried by the flow over the same steps
+        res["accuracy"]["control_kh2d_fp64_vs_fp64_parity"] = curve(kh, args.accuracy_steps, marks2,
+                                                                    ("fp64_parity", "fp64"))
+        res["accuracy"]["control_harris3d_fp64_vs_fp64_parity"] = curve(
+            h3, min(args.accuracy_steps_3d, 300), sorted({10, 100, 300}), ("fp64_parity", "fp64"))
     print(json.dumps(res), flush=True)
     return 0
 
@@ -901,6 +910,8 @@ def main():
                     help="long-run error of the FP32-mixed path against FP64 (KH 2D and Harris 3D)")
     ap.add_argument("--accuracy-steps", type=int, default=2000)
     ap.add_argument("--accuracy-steps-3d", type=int, default=1000)
+    ap.add_argument("--accuracy-control", action="store_true",
+                    help="with --accuracy: also FP64 against FP64 without contraction (round-off growth)")
     args = ap.parse_args()
     if args.accuracy:
         from openmhd_gb300.build import build

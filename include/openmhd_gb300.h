@@ -200,6 +200,11 @@ void omhd_release_host_mirrors(void);
 /* measured FP64 FMA throughput of the current GPU in GFLOP/s (roofline denominator;
  * no counterpart in the reference) */
 int omhd_probe_fp64_peak(double* gflops);
+/* TMA staging of halo tiles in the FP64 pipelined 2D stage kernel (no
+ * counterpart in the reference): on by default; 0 makes the kernel load its
+ * tiles with ordinary loads (same arithmetic, same results), for comparisons.
+ * Library-global: set it before stepping, from one thread. */
+void omhd_set_tma_staging(int enable);
 /* measured FP32 FMA throughput of the current GPU in GFLOP/s (the FP32 roofline
  * denominator of the mixed-precision kernels; no counterpart in the reference) */
 int omhd_probe_fp32_peak(double* gflops);

@@ -22,8 +22,11 @@
 // the namespace so that instantiations built with different floating-point
 // flags never collide at link time.
 #pragma once
+#include <cstring>
+
 #include "omhd_fused.h"
 #include "omhd_step.cuh"
+#include "omhd_tma.h"
 
 #ifndef OMHD_VARIANT
 #error "define OMHD_VARIANT before including omhd_fused2d.cuh"
@@ -132,10 +135,13 @@ __device__ __forceinline__ TileMem<T> tile_mem_separate(unsigned char* smem_raw)
   return m;
 }
 
-// phase A: halo tile load + u2v (+ first GLM half in stage 1); threads t of n
-template <class T, class G>
+// phase A: halo tile load + u2v (+ first GLM half in stage 1); threads t of n.
+// STAGED: the conserved halo tile is already in shared memory (S, laid out as
+// the TMA box: nine planes of RY rows of RX + 2 cells starting one cell left of
+// the halo, so that the box starts on an even x), instead of in global memory.
+template <class T, class G, bool STAGED = false>
 __device__ __forceinline__ void phase_load(const StageArgs& a, int bxi, int byi, const TileMem<T>& m, int t, int n,
-                                           double glmf) {
+                                           double glmf, const double* S = nullptr) {
   constexpr int TX = G::TX, TY = G::TY, RX = G::RX, RY = G::RY, PL = RX * RY;
   const int ix = a.ix, jx = a.jx;
   const size_t N = (size_t)ix * jx;
@@ -159,9 +165,16 @@ __device__ __forceinline__ void phase_load(const StageArgs& a, int bxi, int byi,
       // corners: only the diagonal neighbours are needed, by the resistive terms
       act[b] = q < PL && (cx_in || cy_in || (resist && rx != 0 && rx != RX - 1 && ry != 0 && ry != RY - 1));
       if (act[b]) {
-        const size_t c = (size_t)map_index(gi0 - 2 + rx, ix, perx) + (size_t)ix * map_index(gj0 - 2 + ry, jx, pery);
+        if constexpr (STAGED) {
+          constexpr int SW = RX + 2;
 #pragma unroll
-        for (int v = 0; v < NV; ++v) u[b][v] = __ldg(a.Uin + v * N + c);
+          for (int v = 0; v < NV; ++v) u[b][v] = S[v * (SW * RY) + ry * SW + rx + 1];
+        } else {
+          const size_t c =
+              (size_t)map_index(gi0 - 2 + rx, ix, perx) + (size_t)ix * map_index(gj0 - 2 + ry, jx, pery);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) u[b][v] = __ldg(a.Uin + v * N + c);
+        }
       }
     }
 #pragma unroll
@@ -718,6 +731,18 @@ __device__ __forceinline__ void named_bar_arrive(int id, int n) {
 constexpr size_t pipe_smem_bytes() {
   return sizeof(double) * (size_t)NV * (PipeGeo::RX * PipeGeo::RY + 2 * 2 * (PipeGeo::NXS + PipeGeo::NYS));
 }
+// TMA staging area after the two buffers: the conserved halo tile as one box of
+// (RX + 2) x RY cells x 9 planes, 128-byte aligned (31.7 KB; 226.5 KB in all)
+constexpr int kPipeBoxX = PipeGeo::RX + 2, kPipeBoxY = PipeGeo::RY;
+constexpr unsigned kPipeBoxBytes = sizeof(double) * NV * kPipeBoxX * kPipeBoxY;
+constexpr size_t pipe_stage_off() { return (pipe_smem_bytes() + 127) / 128 * 128; }
+constexpr size_t pipe_smem_bytes_tma() { return pipe_stage_off() + 128 + kPipeBoxBytes; }
+static_assert(pipe_smem_bytes_tma() <= 232448 - 512, "pipelined kernel exceeds the shared memory of one CTA");
+static_assert((kPipeBoxX * 8) % 16 == 0, "TMA box rows must be whole 16-byte units");
+// polls of a TMA completion before a tile is declared lost (well beyond any
+// real transfer; the kernel then records OMHD_TIMEOUT and keeps its barrier
+// protocol, so nothing waits forever)
+constexpr uint32_t kTmaMaxPolls = 1u << 22;
 
 __device__ __forceinline__ TileMem<double> pipe_mem(unsigned char* smem_raw, int b) {
   using G = PipeGeo;
@@ -736,11 +761,13 @@ __device__ __forceinline__ TileMem<double> pipe_mem(unsigned char* smem_raw, int
 }
 
 template <int FLUX, int TAPE, int NPW>
-__global__ void __launch_bounds__(NPW * 32 + PipeGeo::NT, 1) k_stage2d_pipe(const StageArgs a) {
+__global__ void __launch_bounds__(NPW * 32 + PipeGeo::NT, 1)
+    k_stage2d_pipe(const StageArgs a, const __grid_constant__ CUtensorMap tmap, const int use_tma) {
   using G = PipeGeo;
   constexpr int NP = NPW * 32, NC = G::NT, NTOT = NP + NC;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ double red32[32];
+  __shared__ __align__(8) uint64_t tma_bar;
   __shared__ int skip;
   StepState* st = a.st;
   if (threadIdx.x == 0) skip = st->done || *(volatile int*)&a.err->code;
@@ -753,14 +780,50 @@ __global__ void __launch_bounds__(NPW * 32 + PipeGeo::NT, 1) k_stage2d_pipe(cons
   double vmax = 0.0;
   if (threadIdx.x < NP) {  // producers: A, B, wall fixes of tiles blockIdx.x, +gridDim.x, ...
     const int t = threadIdx.x;
+    // TMA staging: a tile whose whole halo lies inside the array (no periodic
+    // wrap, no wall clamp, no ragged edge) arrives as one 3D box load issued
+    // by producer thread 0 while the producers work on the previous tile; the
+    // other tiles take ordinary loads.  The box starts one cell left of the
+    // halo so that its x coordinate is even (8-byte elements, 16-byte rule).
+    unsigned char* s0 = smem_raw + pipe_stage_off();
+    double* S = reinterpret_cast<double*>(s0 + ((128u - (smem_u32(s0) & 127u)) & 127u));  // 128-byte aligned
+    auto staged = [&](int w) {
+      if (!use_tma) return false;
+      const int gi0 = 1 + (w % ntx) * G::TX, gj0 = 1 + (w / ntx) * G::TY;
+      return gi0 >= 3 && gj0 >= 2 && gi0 - 2 + G::RX <= a.ix && gj0 - 2 + G::RY <= a.jx;
+    };
+    auto issue = [&](int w) {
+      const int gi0 = 1 + (w % ntx) * G::TX, gj0 = 1 + (w / ntx) * G::TY;
+      fence_proxy_async_smem();  // the producers' reads of S come before this write
+      mbar_arrive_expect_tx(&tma_bar, kPipeBoxBytes);
+      tma_load_3d(S, &tmap, gi0 - 3, gj0 - 2, 0, &tma_bar);
+    };
+    uint32_t tphase = 0;
+    bool tma_lost = false;
+    if (use_tma) {
+      if (t == 0) mbar_init(&tma_bar, 1);
+      named_bar_sync(kPipeBarProd, NP);
+      if (t == 0 && (int)blockIdx.x < ntiles && staged(blockIdx.x)) issue(blockIdx.x);
+    }
     int i = 0;
     for (int w = blockIdx.x; w < ntiles; w += gridDim.x, ++i) {
       const int b = i & 1;
       const TileMem<double> m = pipe_mem(smem_raw, b);
       if (i >= 2) named_bar_sync(kPipeBarEmpty + b, NTOT);  // consumers are done with buffer b
       if (i >= 1) named_bar_sync(kPipeBarProd, NP);         // W of the previous tile is read
-      phase_load<double, G>(a, w % ntx, w / ntx, m, t, NP, glmf);
+      if (staged(w) && !tma_lost) {
+        if (!mbar_wait_parity(&tma_bar, tphase & 1u, kTmaMaxPolls)) {
+          tma_lost = true;  // recorded; the tile's results are void, the protocol goes on
+          raise_error(a.err, OMHD_TIMEOUT, 1 + (w % ntx) * G::TX, 1 + (w / ntx) * G::TY, 0, 0, 0.0);
+        }
+        ++tphase;
+        phase_load<double, G, true>(a, w % ntx, w / ntx, m, t, NP, glmf, S);
+      } else {
+        phase_load<double, G>(a, w % ntx, w / ntx, m, t, NP, glmf);
+      }
       named_bar_sync(kPipeBarProd, NP);
+      const int wn = w + (int)gridDim.x;
+      if (t == 0 && !tma_lost && wn < ntiles && staged(wn)) issue(wn);
       phase_recon<double, G, TAPE>(a, w % ntx, w / ntx, m, t, NP);
       if (walls) {
         named_bar_sync(kPipeBarProd, NP);
@@ -769,6 +832,7 @@ __global__ void __launch_bounds__(NPW * 32 + PipeGeo::NT, 1) k_stage2d_pipe(cons
       __threadfence_block();
       named_bar_arrive(kPipeBarFull + b, NTOT);
     }
+    if (tma_lost && t == 0) mbar_wait_parity(&tma_bar, tphase & 1u, kTmaMaxPolls);  // a late copy lands first
   } else {  // consumers: C, D of the same tiles, one tile behind
     const int t = threadIdx.x - NP;
     const int nmine = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
@@ -796,7 +860,7 @@ __global__ void __launch_bounds__(NPW * 32 + PipeGeo::NT, 1) k_stage2d_pipe(cons
 
 template <int FLUX, int TAPE, int NPW = 3>
 int launch_pipe(const StageArgs& a, cudaStream_t s) {
-  const size_t bytes = pipe_smem_bytes();
+  const size_t bytes = pipe_smem_bytes_tma();
   static std::atomic<unsigned long long> configured{0};
   int r = set_smem_attr_once(k_stage2d_pipe<FLUX, TAPE, NPW>, bytes, configured);
   if (r) return r;
@@ -806,7 +870,14 @@ int launch_pipe(const StageArgs& a, cudaStream_t s) {
   if (e != cudaSuccess) return (int)e;
   const int ntiles = ((a.ix - 2 + PipeGeo::TX - 1) / PipeGeo::TX) * ((a.jx - 2 + PipeGeo::TY - 1) / PipeGeo::TY);
   const int grid = ntiles < nsm ? ntiles : nsm;
-  k_stage2d_pipe<FLUX, TAPE, NPW><<<grid, NPW * 32 + PipeGeo::NT, bytes, s>>>(a);
+  // the tensor map of this stage's input state (encoded on the host, passed by
+  // value; an array TMA cannot address -- odd ix, unaligned base -- is loaded
+  // with ordinary loads)
+  CUtensorMap tmap;
+  memset(&tmap, 0, sizeof tmap);
+  const int use_tma =
+      tma_staging_enabled() && tma_encode_state_map(&tmap, a.Uin, a.ix, a.jx, NV, kPipeBoxX, kPipeBoxY) == 0;
+  k_stage2d_pipe<FLUX, TAPE, NPW><<<grid, NPW * 32 + PipeGeo::NT, bytes, s>>>(a, tmap, use_tma);
   return (int)cudaGetLastError();
 }
 

@@ -1,12 +1,16 @@
 // omhd_runtime.cu -- library stream, error record and host-pointer mirrors for
 // the routine-level entry points of libopenmhd_gb300.so.
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
 
+#include <cudaTypedefs.h>
+
 #include "omhd_common.cuh"
 #include "omhd_fastmath.h"
 #include "omhd_runtime.h"
+#include "omhd_tma.h"
 
 namespace omhd {
 
@@ -185,11 +189,43 @@ __global__ void k_fastmath_probe(const double* __restrict__ x, long long n, doub
   }
 }
 
+static std::atomic<int> g_tma_on{1};
+bool tma_staging_enabled() { return g_tma_on.load(std::memory_order_relaxed) != 0; }
+
+int tma_encode_state_map(CUtensorMap* map, const double* U, int ix, int jx, int nv, int box_x, int box_y) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    else
+      cudaGetLastError();
+  });
+  if (!encode || !map || !U) return 1;
+  // row pitch and base must be 16-byte aligned; the box's inner extent too
+  if ((ix & 1) || (reinterpret_cast<uintptr_t>(U) & 15) || ((box_x * 8) & 15)) return 2;
+  if (box_x > 256 || box_y > 256 || nv > 256 || box_x > ix || box_y > jx) return 3;
+  const cuuint64_t dims[3] = {(cuuint64_t)ix, (cuuint64_t)jx, (cuuint64_t)nv};
+  const cuuint64_t strides[2] = {(cuuint64_t)ix * 8, (cuuint64_t)ix * (cuuint64_t)jx * 8};
+  const cuuint32_t box[3] = {(cuuint32_t)box_x, (cuuint32_t)box_y, (cuuint32_t)nv};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double*>(U), dims, strides, box, estr,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 0 : 4;
+}
+
 }  // namespace omhd
 
 using namespace omhd;
 
 extern "C" {
+
+void omhd_set_tma_staging(int enable) { g_tma_on.store(enable ? 1 : 0, std::memory_order_relaxed); }
 
 int omhd_probe_fastmath(const double* x, long long n, double* out) {
   if (!x || !out || n < 0) return OMHD_BAD_ARG;
