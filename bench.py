@@ -239,17 +239,77 @@ def cpu_baseline(steps_budget_s: float = 12.0, omp: bool = True, nx: int = NX, n
             "kind": "port", "sample": f"{done} steps of KH {nx}x{ny} after 1 warm-up step ({el:.1f} s)"}, el / done
 
 
+def _omp_threads(n: int) -> None:
+    """Set the OpenMP thread count of this process's OpenMP runtime (shared by
+    the oracle's and the reference translation's libraries)."""
+    import ctypes as C
+
+    try:
+        C.CDLL("libgomp.so.1").omp_set_num_threads(int(n))
+    except OSError:
+        pass
+
+
+def reference_cpu(threads: int, budget_s: float = 12.0, nx: int = NX, ny: int = NY):
+    """The reference's own CPU implementation on the host cores: its 2D_KH
+    driver (2D_KH/main.f90 with u2v, limiter, flux_solver, rk, glm_ss2, set_dt
+    and its bc.f90 walls), translated mechanically to C with the reference's
+    OpenMP directives (oracle/ref.py), at the configuration's grid, started
+    from the configuration's seeded KH state instead of 2D_KH/model.f90.  The
+    reference assumes dy = dx, so its y spacing is the x spacing here: the same
+    work per cell-update on a squeezed domain.  Timed as the difference of two
+    runs of the driver (2 and 2 + K steps: the first two steps, which touch the
+    work arrays first, cancel).  Returns None when the translation is absent."""
+    from oracle import oracle, ref
+
+    if not ref.buildable():
+        return None
+    ref.build("2D_KH")
+    from openmhd_gb300 import kelvin_helmholtz
+
+    cfg, model = kelvin_helmholtz(nx, ny, precision="fp64")
+    g = oracle.Grid.from_solver_config(cfg)
+    g.model(model.kind, amp=model.amp, bx0=model.bx0, pert=model.pert, seed=model.seed)
+    ref.set_initial_2d("2D_KH", g.U, g.x, g.y, cfg.dx)
+    del g
+    _omp_threads(threads)
+    run = dict(ix=cfg.ix, jx=cfg.jx, tend=1e30, dtout=1e30, cfl=cfg.cfl, lm_type=1, flux_type=3, time_type=0)
+
+    def timed(nsteps):
+        t0 = time.perf_counter()
+        st, _ = ref.run_main("2D_KH", loop_max=nsteps + 1, **run)
+        if st:
+            raise RuntimeError(f"the reference driver stopped (line {st})")
+        return time.perf_counter() - t0
+
+    t2 = timed(2)
+    t3 = timed(3)
+    per_step = max(t3 - t2, 1e-9)
+    k = int(min(30, max(3, budget_s / per_step)))
+    tk = timed(2 + k)
+    el = tk - t2
+    ref.set_initial_2d("2D_KH")
+    _omp_threads(os.cpu_count() or 1)
+    return {"value": nx * ny * k / el, "unit": "cell-updates/s", "cores": threads, "kind": "reference",
+            "sample": f"{k} steps of the reference's 2D_KH driver (translated to C, OpenMP, {threads} threads) at "
+                      f"{nx}x{ny} from the configuration's KH state, after 2 warm-up steps ({el:.1f} s)"}
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
         return 0
-    base, _ = cpu_baseline(steps_budget_s=min(60.0, max(8.0, 4.0 * args.steps)))
+    cores = os.cpu_count() or 1
+    base = reference_cpu(cores, budget_s=min(60.0, max(8.0, 4.0 * args.steps)))
+    if base is None:  # no translation of the reference here: the oracle port on all cores
+        base, _ = cpu_baseline(steps_budget_s=min(60.0, max(8.0, 4.0 * args.steps)))
     line = {
         "impl": "reference", "metric": "cell-updates/s", "value": base["value"], "unit": "cell-updates/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "precision": "fp64",
-                   "note": "reference is Fortran (no compiler here or on the box): C restatement, OpenMP"},
+                   "note": "reference is Fortran (no compiler here or on the box): its own source translated "
+                           "mechanically to C (oracle/ref.py), OpenMP; else the C restatement"},
         "cpu_baseline": base,
         "e2e": {"value": base["value"], "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -425,9 +485,17 @@ def run_ours(args):
     if not args.no_sq:
         line["ot4096sq"] = _leg(run_sq4096, args, fp64_peak)
     if rank == 0 and not args.no_cpu_baseline:
-        base = _leg(lambda: cpu_baseline(steps_budget_s=10.0)[0])
-        if "error" not in base:  # the same oracle on one core, beside the all-core figure
-            base["serial"] = _leg(lambda: cpu_baseline(steps_budget_s=4.0, omp=False)[0])
+        cores = os.cpu_count() or 1
+        base = _leg(lambda: reference_cpu(cores, budget_s=10.0))
+        if base is None or "error" in base:  # the oracle port, where the translation is absent
+            if base is not None:
+                line["reference_cpu_error"] = base["error"]
+            base = _leg(lambda: cpu_baseline(steps_budget_s=10.0)[0])
+            if "error" not in base:  # the same oracle on one core, beside the all-core figure
+                base["serial"] = _leg(lambda: cpu_baseline(steps_budget_s=4.0, omp=False)[0])
+        else:  # the reference on one core, and the oracle port beside it
+            base["serial"] = _leg(lambda: reference_cpu(1, budget_s=12.0))
+            base["port"] = _leg(lambda: cpu_baseline(steps_budget_s=6.0)[0])
         line["cpu_baseline"] = base
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -25,6 +25,12 @@ What is translated, and how (the choices follow gfortran's code generation):
   active call), continue; write and format statements are dropped (the
   reference's diagnostics), and so is any statement carrying a numeric label
   reference such as open(...,err=100);
+* OpenMP directives (!$omp): parallel do with private / reduction / collapse
+  clauses (a reduction on a dummy argument goes through a local copy; private
+  arrays start from their values before the loop, the serial semantics),
+  parallel regions with do, workshare (as single) and barrier, as the
+  corresponding C pragmas; fixed-size local arrays become C arrays, so that
+  they can be private to a thread;
 * expressions: Fortran precedence (** right-associative, unary sign on the
   first term of an additive expression), integer and real(8) arithmetic mapped
   to the same C types (C's usual conversions match Fortran's mixed-mode rules
@@ -118,7 +124,22 @@ def read_statements(path: str, include_dir: str | None = None) -> list[Stmt]:
         raw = f.read().splitlines()
     stmts: list[Stmt] = []
     buf, start = "", 0
+    dbuf, dstart = None, 0
     for n, line in enumerate(raw, 1):
+        ls = line.strip()
+        if ls.lower().startswith("!$omp"):  # OpenMP directive (continued with a trailing &)
+            d = ls[5:].strip()
+            cont = d.endswith("&")
+            if cont:
+                d = d[:-1].strip()
+            if dbuf is None:
+                dbuf, dstart = d, n
+            else:
+                dbuf += " " + d
+            if not cont:
+                stmts.append(Stmt("!$omp " + _lower_outside_strings(dbuf), None, os.path.basename(path), dstart))
+                dbuf = None
+            continue
         body = _strip_comment(line).rstrip()
         if not body.strip():
             if buf:
@@ -619,6 +640,8 @@ class Emitter:
         self.hooks = hooks
         self.out: list[str] = []
         self.tmp = 0
+        self.omp_pending = None  # (pragma kind, clause text) for the next do loop
+        self.shadow: dict = {}   # dummy scalar -> local copy inside an OpenMP reduction
 
     # -- helpers --
     def fresh(self, base="_t"):
@@ -629,6 +652,8 @@ class Emitter:
         return f"{self.prefix}{name}"
 
     def var(self, sym: Sym) -> str:
+        if sym.name in self.shadow:
+            return self.shadow[sym.name]
         if sym.dummy and not sym.dims and sym.type != "char":
             return f"(*{sym.name})"
         if self.u.kind == "function" and sym.name == self.u.name:
@@ -897,8 +922,119 @@ class Emitter:
     def emit(self, line: str, depth: int):
         self.out.append("  " * depth + line)
 
+    def const_int(self, e):
+        """Value of an integer expression of literals and (not overridden)
+        parameters, or None."""
+        if isinstance(e, Num):
+            return int(e.text) if e.type == "int" else None
+        if isinstance(e, Name):
+            sym = self.lookup(e.name)
+            if sym is None or not sym.param or sym.dims or sym.type != "int" or e.name in self.param_override:
+                return None
+            return self.const_int(sym.init)
+        if isinstance(e, Un) and e.op == "-":
+            v = self.const_int(e.a)
+            return None if v is None else -v
+        if isinstance(e, Bin) and e.op in ("+", "-", "*"):
+            x, y = self.const_int(e.a), self.const_int(e.b)
+            if x is None or y is None:
+                return None
+            return x + y if e.op == "+" else (x - y if e.op == "-" else x * y)
+        return None
+
+    def const_size(self, s: Sym):
+        n = 1
+        for lo, hi in s.dims:
+            a, b = self.const_int(lo), self.const_int(hi)
+            if a is None or b is None:
+                return None
+            n *= max(b - a + 1, 0)
+        return n
+
+    def omp_clauses(self, text: str, depth: int) -> tuple[str, list]:
+        """C clauses for an OpenMP directive's clause text, and the (dummy,
+        local copy) pairs of reductions on dummy arguments."""
+        out, copies = [], []
+        for name, args in re.findall(r"([a-z_]+)\s*\(([^)]*)\)", text):
+            if name == "private":
+                # private scalars start undefined, as in Fortran; private arrays
+                # start from the values they hold before the region
+                # (firstprivate): the serial program's values, which the
+                # reference relies on for entries its loops never set (e.g. the
+                # side fluxes' normal-field slot zeroed before the face loop)
+                keep, arrays = [], []
+                for v in [x.strip() for x in args.split(",") if x.strip()]:
+                    sym = self.lookup(v)
+                    if sym is None:
+                        raise TranslateError(f"private {v} is not declared")
+                    if sym.dims and v not in self.fixed:
+                        raise TranslateError(f"private array {v} has no fixed size")
+                    if sym.dummy or sym.param:
+                        continue
+                    (arrays if sym.dims else keep).append(v)
+                if keep:
+                    out.append(f"private({', '.join(keep)})")
+                if arrays:
+                    out.append(f"firstprivate({', '.join(arrays)})")
+            elif name == "reduction":
+                op, names = args.split(":", 1)
+                op = op.strip()
+                cop = {"max": "max", "min": "min", "+": "+"}.get(op)
+                if cop is None:
+                    raise TranslateError(f"reduction {op} is not part of the subset")
+                vs = []
+                for v in [x.strip() for x in names.split(",") if x.strip()]:
+                    sym = self.lookup(v)
+                    if sym.dummy:
+                        loc = self.fresh("_red")
+                        ct = "double" if sym.type == "double" else "int"
+                        self.emit(f"{ct} {loc} = (*{v});", depth)
+                        copies.append((v, loc))
+                        vs.append(loc)
+                    else:
+                        vs.append(v)
+                out.append(f"reduction({cop}:{', '.join(vs)})")
+            elif name == "collapse":
+                out.append(f"collapse({int(args)})")
+            elif name in ("shared", "firstprivate", "schedule", "default"):
+                out.append(f"{name}({args})")
+            else:
+                raise TranslateError(f"OpenMP clause {name} is not part of the subset")
+        return " ".join(out), copies
+
+    def omp_directive(self, t: str, depth: int):
+        d = t[len("!$omp"):].strip()
+        if re.match(r"end\b", d):
+            rest = d[3:].strip()
+            if rest in ("parallel do", "do"):
+                return
+            if rest in ("parallel", "workshare"):
+                self.emit("}", depth)
+                return
+            raise TranslateError(f"unsupported directive !$omp {d}")
+        if d.startswith("parallel do"):
+            self.omp_pending = ("parallel for", d[len("parallel do"):])
+        elif d.startswith("parallel"):
+            clauses, copies = self.omp_clauses(d[len("parallel"):], depth)
+            if copies:
+                raise TranslateError("reductions on dummies need a parallel do")
+            self.emit(f"#pragma omp parallel {clauses}".rstrip(), depth)
+            self.emit("{", depth)
+        elif d.startswith("do"):
+            self.omp_pending = ("for", d[2:])
+        elif d == "workshare":  # one thread does the work; implicit barrier at its end
+            self.emit("#pragma omp single", depth)
+            self.emit("{", depth)
+        elif d == "barrier":
+            self.emit("#pragma omp barrier", depth)
+        else:
+            raise TranslateError(f"unsupported directive !$omp {d}")
+
     def unit(self, u: Unit):
         self.u = u
+        self.fixed = set()
+        self.omp_pending = None
+        self.shadow = {}
         self.param_override = dict(self.overrides.get("program", {})) if u.kind == "program" else {}
         ps = []
         for a in u.args:
@@ -938,9 +1074,14 @@ class Emitter:
                     self.emit(f"const {ct} {s.name} = {val};", 1)
                 continue
             if s.dims:
-                size = " * ".join(f"(long)({ext})" for _, ext in self.dim_bounds(s))
                 if s.saved:
                     raise TranslateError(f"{u.name}: saved array {s.name} is not supported")
+                n = self.const_size(s)
+                if n is not None and n <= 65536:  # fixed size: a C array (private per thread if asked)
+                    self.emit(f"{ct} {s.name}[{n}] = {{0}};", 1)
+                    self.fixed.add(s.name)
+                    continue
+                size = " * ".join(f"(long)({ext})" for _, ext in self.dim_bounds(s))
                 self.emit(f"{ct}* {s.name} = ({ct}*)calloc((size_t)({size}), sizeof({ct}));", 1)
                 frees.append(s.name)
                 continue
@@ -998,6 +1139,9 @@ class Emitter:
         t = st.text
         self.st = st
         try:
+            if t.startswith("!$omp"):
+                self.omp_directive(t, depth)
+                return k + 1
             if self._is_if_then(t):
                 end, mids = self._match_end(body, k, b, self._is_if_then,
                                             lambda x: bool(re.match(r"end\s*if$", x)),
@@ -1022,18 +1166,51 @@ class Emitter:
                 m = re.match(r"do\s+([a-z_]\w*)\s*=\s*(.*)$", t)
                 if not m:
                     raise TranslateError(f"unsupported loop form: {t}")
-                v = self.lookup(m.group(1))
-                parts = split_top(m.group(2), ",")
-                lo, hi = self.expr(parse_expr(parts[0])), self.expr(parse_expr(parts[1]))
-                step = parts[2] if len(parts) > 2 else "1"
-                stp = int(step)
-                a_, b_ = self.fresh("_lo"), self.fresh("_hi")
-                vv = self.var(v)
-                cmp = "<=" if stp > 0 else ">="
-                self.emit(f"{{ const int {a_} = {lo}, {b_} = {hi};", depth)
-                self.emit(f"for ({vv} = {a_}; {vv} {cmp} {b_}; {vv} += {stp}) {{", depth)
-                self.block(body, k + 1, end, depth + 1)
+                pending, self.omp_pending = self.omp_pending, None
+                ncol = 1
+                copies = []
+                if pending:
+                    mm = re.search(r"collapse\s*\(\s*(\d+)\s*\)", pending[1])
+                    ncol = int(mm.group(1)) if mm else 1
+                # the loop nest the directive covers (collapse: perfectly nested loops)
+                nest, kk, ee = [], k, end
+                for lev in range(ncol):
+                    tt = body[kk].text
+                    mm = re.match(r"do\s+([a-z_]\w*)\s*=\s*(.*)$", tt)
+                    if not mm:
+                        raise TranslateError(f"unsupported loop form: {tt}")
+                    nest.append((self.lookup(mm.group(1)), split_top(mm.group(2), ",")))
+                    if lev + 1 < ncol:
+                        e2, _ = self._match_end(body, kk + 1, ee, self._is_do,
+                                                lambda x: bool(re.match(r"end\s*do$", x)))
+                        if not self._is_do(body[kk + 1].text) or e2 != ee - 1:
+                            raise TranslateError("collapse needs perfectly nested loops")
+                        kk, ee = kk + 1, e2
+                heads = []
+                bounds = []
+                for sym, parts in nest:
+                    lo, hi = self.expr(parse_expr(parts[0])), self.expr(parse_expr(parts[1]))
+                    stp = int(parts[2]) if len(parts) > 2 else 1
+                    a_, b_ = self.fresh("_lo"), self.fresh("_hi")
+                    vv = self.var(sym)
+                    cmp = "<=" if stp > 0 else ">="
+                    bounds.append(f"{a_} = {lo}, {b_} = {hi}")
+                    heads.append(f"for ({vv} = {a_}; {vv} {cmp} {b_}; {vv} += {stp})")
+                if pending:  # local copies of reduced dummies are declared before the loop's block
+                    clauses, copies = self.omp_clauses(pending[1], depth)
+                    for dv, loc in copies:
+                        self.shadow[dv] = loc
+                self.emit(f"{{ const int {', '.join(bounds)};", depth)
+                if pending:
+                    self.emit(f"#pragma omp {pending[0]} {clauses}".rstrip(), depth)
+                for h in heads[:-1]:
+                    self.emit(h, depth)
+                self.emit(heads[-1] + " {", depth)
+                self.block(body, kk + 1, ee, depth + 1)
                 self.emit("} }", depth)
+                for dv, loc in copies:
+                    del self.shadow[dv]
+                    self.emit(f"(*{dv}) = {loc};", depth)
                 return end + 1
             if re.match(r"select\s+case\s*\(", t):
                 end, mids = self._match_end(body, k, b, lambda x: bool(re.match(r"select\s+case\s*\(", x)),

@@ -8,7 +8,8 @@ reference's serial CPU path cannot be compiled as it stands.  This recipe runs
 oracle/f90sub.py over the reference's own source files of four problem
 directories, exactly as they lie in the OpenMHD checkout, and compiles the C it
 produces (with oracle/ref_harness.c, which records the driver's snapshots)
-into oracle/_ref/lib<problem>.so:
+into oracle/_ref/lib<problem>.so (OpenMP on the loops the reference marks
+!$omp, so the drivers run on all host cores):
 
   2D_basic         main.f90, model.f90 (Orszag-Tang), u2v, limiter, flux_solver,
                    rk, glm_ss2, set_dt, bc
@@ -22,8 +23,11 @@ The main program's size and run parameters (ix, jx, kx, loop_max, tend,
 dtout, cfl, lm_type, flux_type, time_type), which a user of the reference sets
 by editing main.f90, are read at run time from slots this module fills, so one
 library serves every grid the tests use.  The snapshot writer
-(fileio_output) becomes a call into the harness.  Everything else is the
-reference's code.
+(fileio_output) becomes a call into the harness, and a 2D driver's model call
+can take an injected initial state (set_initial_2d: the benchmark runs the
+reference's KH driver from the configuration's own state).  Everything else is
+the reference's code.  Without the checkout (the GPU host), the translation
+already in oracle/_ref/ is compiled as it is.
 
     python -m oracle.ref <path of the OpenMHD checkout>      # build all four
 """
@@ -51,7 +55,7 @@ PROBLEMS = {
 }
 IPAR = {"ix": 0, "jx": 1, "kx": 2, "loop_max": 3, "lm_type": 4, "flux_type": 5, "time_type": 6}
 DPAR = {"tend": 0, "dtout": 1, "cfl": 2}
-CFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-std=gnu11", "-fPIC", "-w"]
+CFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-std=gnu11", "-fPIC", "-fopenmp", "-w"]
 
 
 def available(reference: str | None = None) -> bool:
@@ -76,7 +80,9 @@ def translate(problem: str, reference: str | None = None) -> str:
     for name, k in DPAR.items():
         overrides["program"][name] = f"(f90_dpar_set[{k}] ? f90_dpar[{k}] : ({{orig}}))"
     if nd == 2:
-        hooks = {"fileio_output": ("ref_snapshot_2d", [1, 2, 3, 4, 5, 6, 7], ["dx", "dt", "ch"])}
+        hooks = {"fileio_output": ("ref_snapshot_2d", [1, 2, 3, 4, 5, 6, 7], ["dx", "dt", "ch"]),
+                 # the driver's model call may take an injected initial state instead
+                 "model": ("ref_model_2d", [0, 1, 2, 3, 4, 5, 6], [])}
     else:
         hooks = {"fileio_output": ("ref_snapshot_3d", [1, 2, 3, 4, 5, 6, 7, 8, 9], ["dx", "dt", "ch"])}
     header = (f"/* generated by oracle/f90sub.py from the reference's {problem}/"
@@ -84,20 +90,37 @@ def translate(problem: str, reference: str | None = None) -> str:
     return f90sub.emit_c(units, "f90_", overrides, hooks, header)
 
 
+def translated(problem: str) -> bool:
+    """True when the C translation of `problem` is present in oracle/_ref/
+    (made where the checkout exists; it travels with the working tree)."""
+    return os.path.isfile(os.path.join(OUT, f"{problem}.c"))
+
+
 def build(problem: str, reference: str | None = None, force: bool = False) -> str:
+    """Translate (when the checkout is present) and compile one problem
+    directory; without the checkout, compile the translation already in
+    oracle/_ref/."""
     reference = reference or REFERENCE
     so = lib_path(problem)
-    srcs = [os.path.join(reference, problem, f) for f in PROBLEMS[problem][1]]
-    deps = srcs + [os.path.join(HERE, "f90sub.py"), os.path.join(HERE, "ref_harness.c"), __file__]
+    c_path = os.path.join(OUT, f"{problem}.c")
+    have_src = os.path.isfile(os.path.join(reference, problem, "main.f90"))
+    if have_src:
+        srcs = [os.path.join(reference, problem, f) for f in PROBLEMS[problem][1]]
+        deps = srcs + [os.path.join(HERE, "f90sub.py"), os.path.join(HERE, "ref_harness.c"), __file__]
+    elif os.path.isfile(c_path):
+        deps = [c_path, os.path.join(HERE, "ref_harness.c")]
+    else:
+        raise FileNotFoundError(f"neither the OpenMHD checkout nor {c_path} is present")
     if not force and os.path.exists(so) and all(os.path.getmtime(p) <= os.path.getmtime(so) for p in deps):
         return so
     os.makedirs(OUT, exist_ok=True)
-    c_path = os.path.join(OUT, f"{problem}.c")
-    with open(c_path, "w") as f:
-        f.write(translate(problem, reference))
+    if have_src:
+        with open(c_path, "w") as f:
+            f.write(translate(problem, reference))
     tmp = so + ".tmp"
-    cmd = [os.environ.get("CC", "gcc")] + CFLAGS + ["-shared", "-o", tmp, c_path,
-                                                    os.path.join(HERE, "ref_harness.c"), "-lm"]
+    nd = PROBLEMS[problem][0]
+    cmd = [os.environ.get("CC", "gcc")] + CFLAGS + (["-DREF_MODEL_HOOK_2D"] if nd == 2 else []) + [
+        "-shared", "-o", tmp, c_path, os.path.join(HERE, "ref_harness.c"), "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"compiling the translated {problem} failed:\n{r.stderr[-4000:]}")
@@ -107,6 +130,26 @@ def build(problem: str, reference: str | None = None, force: bool = False) -> st
 
 def build_all(reference: str | None = None, force: bool = False) -> list[str]:
     return [build(p, reference, force) for p in PROBLEMS]
+
+
+def buildable(reference: str | None = None) -> bool:
+    return available(reference) or all(translated(p) for p in PROBLEMS)
+
+
+def set_initial_2d(problem: str, U=None, x=None, y=None, dx: float = 0.0) -> None:
+    """Make the 2D driver of `problem` start from U (reference layout, ghosts
+    included) with coordinates x, y and spacing dx instead of running its
+    model.f90; U=None restores the driver's own model."""
+    lib = load(problem)
+    if U is None:
+        lib.ref_set_initial_2d(None, None, None, C.c_double(0.0), 0, 0)
+        return
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    if lib.ref_set_initial_2d(C.c_void_p(U.ctypes.data), C.c_void_p(x.ctypes.data), C.c_void_p(y.ctypes.data),
+                              C.c_double(dx), int(U.shape[-1]), int(U.shape[-2])):
+        raise MemoryError("could not keep the initial state")
 
 
 _libs: dict = {}
