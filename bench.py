@@ -899,6 +899,10 @@ def run_profile(args):
 
     from openmhd_gb300 import Solver, harris3d, kelvin_helmholtz
 
+    if args.one_role_3d:
+        from openmhd_gb300 import _lib
+
+        _lib.load().omhd_set_3d_pipeline(0)
     if args.nz:
         cfg, model = harris3d(args.nx, args.ny, args.nz, precision=args.precision)
     else:
@@ -974,6 +978,8 @@ def main():
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--nz", type=int, default=0)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_parity", "mixed"])
+    ap.add_argument("--one-role-3d", action="store_true",
+                    help="with --profile: the one-role FP64 3D stage kernel instead of the warp-specialised one")
     ap.add_argument("--accuracy", action="store_true",
                     help="long-run error of the FP32-mixed path against FP64 (KH 2D and Harris 3D)")
     ap.add_argument("--accuracy-steps", type=int, default=2000)

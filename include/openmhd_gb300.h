@@ -205,6 +205,11 @@ int omhd_probe_fp64_peak(double* gflops);
  * tiles with ordinary loads (same arithmetic, same results), for comparisons.
  * Library-global: set it before stepping, from one thread. */
 void omhd_set_tma_staging(int enable);
+/* The warp-specialised FP64 3D stage kernel (HLLD with minmod or MC; no
+ * counterpart in the reference): on by default; 0 selects the one-role 3D
+ * kernel (same scheme; results agree to rounding), for comparisons.
+ * Library-global: set it before stepping, from one thread. */
+void omhd_set_3d_pipeline(int enable);
 /* measured FP32 FMA throughput of the current GPU in GFLOP/s (the FP32 roofline
  * denominator of the mixed-precision kernels; no counterpart in the reference) */
 int omhd_probe_fp32_peak(double* gflops);

@@ -858,7 +858,11 @@ __global__ void __launch_bounds__(NPW * 32 + PipeGeo::NT, 1)
   }
 }
 
-template <int FLUX, int TAPE, int NPW = 3>
+// producer warps of the pipelined kernel (a build-time constant, for tuning)
+#ifndef OMHD_PIPE_PRODUCER_WARPS
+#define OMHD_PIPE_PRODUCER_WARPS 3
+#endif
+template <int FLUX, int TAPE, int NPW = OMHD_PIPE_PRODUCER_WARPS>
 int launch_pipe(const StageArgs& a, cudaStream_t s) {
   const size_t bytes = pipe_smem_bytes_tma();
   static std::atomic<unsigned long long> configured{0};

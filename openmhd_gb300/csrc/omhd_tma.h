@@ -84,4 +84,8 @@ int tma_encode_state_map(CUtensorMap* map, const double* U, int ix, int jx, int 
 // staged and the ordinary-load paths bit for bit.
 bool tma_staging_enabled();
 
+// Library-wide switch of the warp-specialised FP64 3D stage kernel (on by
+// default; off: the one-role kernel), for comparisons in tests.
+bool pipe3d_enabled();
+
 }  // namespace omhd
