@@ -9,10 +9,13 @@ steps.  Synthetic seeded initial data (no external dataset exists).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Prints one JSON line (rank 0).  --impl reference times the CPU restatement of
-the reference's serial Fortran path (the oracle port, OpenMP over all host
-cores) on the same workload.  Multi-GPU runs are independent replicas, one per
-GPU ("replicas only": the path has no exchange once one GPU holds a grid).
+Prints one JSON line (rank 0).  --impl reference times the reference's own
+CPU code on all host cores: its 2D_KH driver, translated mechanically from the
+Fortran to C with its OpenMP directives (oracle/ref.py), at this grid from the
+same seeded state; where that translation is absent, the C restatement of the
+reference's path (the oracle port, OpenMP).  Multi-GPU runs are independent
+replicas, one per GPU ("replicas only": the path has no exchange once one GPU
+holds a grid).
 """
 from __future__ import annotations
 
@@ -946,16 +949,45 @@ def run_profile_adjoint(args):
 
 def run_profile_batched(args):
     """Small fixed ensemble run for profiler captures: 16 members, sides
-    {256..512}, FP32-mixed, --steps steps with the 32x8 tiling, 2 CTAs/SM."""
+    {256..512}, --precision (fp64 or mixed), --steps steps with the 32x8 tiling,
+    2 CTAs per SM for FP32-mixed, 1 for FP64."""
     from openmhd_gb300.ensemble import Ensemble, batched_problem_set
 
-    cfgs, models = batched_problem_set(16, seed=1, precision="mixed", sides=[256, 320, 384, 448, 512])
+    prec = "mixed" if args.precision == "mixed" else "fp64"
+    cfgs, models = batched_problem_set(16, seed=1, precision=prec, sides=[256, 320, 384, 448, 512])
     ens = Ensemble(cfgs).init_models(models)
-    ens.set_tiling(0, 2)
+    ens.set_tiling(0, 2 if prec == "mixed" else 1)
     ens.step(args.steps)
     infos = ens.sync()
-    print(json.dumps({"profile": "batched", "members": len(cfgs), "cells": ens.cells, "steps": args.steps,
-                      "status": max(i.status for i in infos)}), flush=True)
+    print(json.dumps({"profile": "batched", "precision": prec, "members": len(cfgs), "cells": ens.cells,
+                      "steps": args.steps, "status": max(i.status for i in infos)}), flush=True)
+    return 0
+
+
+def run_profile_routines(args):
+    """Small fixed run of the routine-level drop-in kernels for profiler
+    captures: u2v, limiter (x, every variable of V) and flux_solver (x, HLLD)
+    on an Orszag-Tang state of --nx x --ny cells held on the device, --steps
+    times."""
+    import torch
+
+    from openmhd_gb300 import Solver, orszag_tang, routines
+
+    cfg, model = orszag_tang(args.nx, args.ny, precision="fp64")
+    U = Solver(cfg).init_model(model).U.clone()
+    V = torch.empty((4,) + tuple(U.shape[1:]), dtype=torch.float64, device="cuda")
+    VL = torch.empty_like(U)
+    VR = torch.empty_like(U)
+    F = torch.empty_like(U)
+    for _ in range(args.steps):
+        routines.u2v(U, V)
+        for v in range(4):
+            routines.limiter(V[v], VL[v], VR[v], 1, 2)
+        for v in range(4, 9):
+            routines.limiter(U[v], VL[v], VR[v], 1, 2)
+        routines.flux_solver(F, VL, VR, 1.0, 1, 3)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "routines", "nx": args.nx, "ny": args.ny, "steps": args.steps}), flush=True)
     return 0
 
 
@@ -974,6 +1006,8 @@ def main():
     ap.add_argument("--profile", action="store_true", help="small fixed run for profiler captures")
     ap.add_argument("--profile-adjoint", action="store_true", help="small adjoint run for profiler captures")
     ap.add_argument("--profile-batched", action="store_true", help="small ensemble run for profiler captures")
+    ap.add_argument("--profile-routines", action="store_true",
+                    help="routine-level drop-in kernels (u2v, limiter, flux_solver) for profiler captures")
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--nz", type=int, default=0)
@@ -992,7 +1026,7 @@ def main():
 
         build()
         return run_accuracy(args)
-    if args.profile or args.profile_adjoint or args.profile_batched:
+    if args.profile or args.profile_adjoint or args.profile_batched or args.profile_routines:
         from openmhd_gb300.build import build
 
         build()
@@ -1000,6 +1034,8 @@ def main():
             return run_profile_adjoint(args)
         if args.profile_batched:
             return run_profile_batched(args)
+        if args.profile_routines:
+            return run_profile_routines(args)
         return run_profile(args)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

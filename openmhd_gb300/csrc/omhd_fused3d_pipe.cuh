@@ -13,10 +13,12 @@
 //     x-oriented FP64 HLLD solver (y and z faces rotated into x orientation),
 //     the resistive face terms (3D_reconnection_gpu/flux_resistive.cuf), and
 //     the update of plane p (rk.f90) with the owner-writes ghost fill, GLM and
-//     the CFL reduction in stage 2.
+//     the CFL reduction in stage 2 (by the consumers that own cells; the others
+//     go on to the next plane's faces meanwhile).
 // Two face-state buffers change hands through named barriers (FULL[b]:
-// producers arrive, consumers wait; EMPTY[b]: consumers arrive after the
-// update, producers wait before refilling b); fluxes overwrite the lower-cell
+// producers arrive, consumers wait -- split into the consumers that own cells
+// and the others; EMPTY[b]: consumers arrive when done with b, producers wait
+// before refilling b); fluxes overwrite the lower-cell
 // face state that only their own face reads; the z flux of face p-1/2 is kept
 // per cell in shared memory (Fzm).  The ring holds planes p-1 .. p+3: the
 // consumers read p-1 .. p+1 (resistive terms) while the producers write p+3
@@ -37,9 +39,26 @@ constexpr int NRING = 5;
 constexpr int XS = TX + 2, NXS = TY * XS;  // x-reconstructed cells (rows of TX+2)
 constexpr int NYS = (TY + 2) * TX;         // y-reconstructed cells (columns of TY+2)
 constexpr int NXF = TY * (TX + 1), NYF = (TY + 1) * TX, NZF = NCELL;
-constexpr int ZC = 64;  // planes per CTA
-constexpr int NPW = 3, NP = NPW * 32, NC = 288, NTOT = NP + NC;
-constexpr int kBarProd = 1, kBarCons = 2, kBarFull = 3, kBarEmpty = 5;
+// planes per CTA and the producer / consumer warp split (build-time constants, for tuning)
+#ifndef OMHD_PIPE3D_ZCHUNK
+#define OMHD_PIPE3D_ZCHUNK 128
+#endif
+#ifndef OMHD_PIPE3D_PRODUCER_WARPS
+#define OMHD_PIPE3D_PRODUCER_WARPS 3
+#endif
+constexpr int ZC = OMHD_PIPE3D_ZCHUNK;
+constexpr int NPW = OMHD_PIPE3D_PRODUCER_WARPS, NP = NPW * 32, NC = (12 - NPW) * 32, NTOT = NP + NC;
+// named barriers: producers; per buffer b: FULL_OWN[b] (producers arrive, the
+// consumers that own cells wait), FULL_NON[b] (producers arrive, the other
+// consumers wait), EMPTY[b] (all consumers arrive, producers wait) and
+// CONS[b] (the cell owners wait for every consumer's fluxes; the others only
+// arrive).  The consumers without cells thus start plane p+1's faces while the
+// owners update plane p; each barrier is used again two planes later, and the
+// producers can re-arm a buffer's barriers only after EMPTY[b], which the
+// owners release after their update, so no generation is overtaken.
+constexpr int kBarProd = 1, kBarFull = 3, kBarEmpty = 5, kBarCons = 7, kBarFullNon = 9;
+constexpr int NOWN = NCELL, NNON = NC - NCELL;  // consumer threads that own a cell / own none
+static_assert(NOWN % 32 == 0 && NNON % 32 == 0 && NNON > 0, "owner split must be whole warps");
 // one buffer: SLx, SRx [NV][NXS], SLy, SRy [NV][NYS], SLz, SRz [NV][NZF]
 constexpr int BUF = NV * 2 * (NXS + NYS + NZF);
 constexpr size_t kSmemDoubles = (size_t)NRING * NV * PL + 2 * (size_t)BUF + (size_t)NV * NCELL;
@@ -317,7 +336,8 @@ __global__ void __launch_bounds__(NTOT, 1) k_stage3d_pipe(const StageArgs a) {
         }
       }
       __threadfence_block();
-      bar_arrive(kBarFull + b, NTOT);
+      bar_arrive(kBarFull + b, NP + NOWN);
+      bar_arrive(kBarFullNon + b, NP + NNON);
     }
   } else {
     // ======================= consumers =======================
@@ -327,7 +347,10 @@ __global__ void __launch_bounds__(NTOT, 1) k_stage3d_pipe(const StageArgs a) {
     for (int i = 0; i < nplanes; ++i) {
       const int p = k0 + i, b = i & 1;
       const Buf m = buf_at(bufbase + (size_t)b * BUF);
-      bar_sync(kBarFull + b, NTOT);
+      if (t < NOWN)
+        bar_sync(kBarFull + b, NP + NOWN);
+      else
+        bar_sync(kBarFullNon + b, NP + NNON);
       // ---- fluxes of the 136 x, 144 y and 128 z faces, x-oriented ----
       for (int q = t; q < NXF + NYF + NZF; q += NC) {
         const int dir = q < NXF ? 1 : (q < NXF + NYF ? 2 : 3);
@@ -420,7 +443,19 @@ __global__ void __launch_bounds__(NTOT, 1) k_stage3d_pipe(const StageArgs a) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) bl[v * sv] = F[v];
       }
-      bar_sync(kBarCons, NC);
+      // Only threads t < NCELL update cells.  The others have no further use of
+      // this buffer: they signal both barriers without waiting (bar.arrive
+      // counts toward the same totals) and go on to the next plane's faces,
+      // which overlaps the update.
+      if (t >= NOWN) {
+        bar_arrive(kBarCons + b, NC);
+        if (i + 2 < nplanes) {
+          __threadfence_block();
+          bar_arrive(kBarEmpty + b, NTOT);
+        }
+        continue;
+      }
+      bar_sync(kBarCons + b, NC);
       // ---- update plane p ----
       for (int c = t; c < NCELL; c += NC) {
         const int tx = c % TX, ty = c / TX;

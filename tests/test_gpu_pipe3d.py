@@ -30,8 +30,8 @@ def _oracle_pair(cfg, model=None, U=None):
 
 @pytest.mark.parametrize("limiter", ["mc", "minmod"])
 def test_harris_multichunk_ragged_vs_oracle(cuda_lib, oracle_mod, limiter):
-    """Resistive Harris sheet 136x68x136: ragged 16x8 columns in x and y, three
-    z chunks (64, 64, 8 planes), conducting z walls; 1 step within 1e-12 and 3
+    """Resistive Harris sheet 136x68x136: ragged 16x8 columns in x and y, two
+    z chunks (128 and 8 planes), conducting z walls; 1 step within 1e-12 and 3
     steps within 1e-10 of the oracle."""
     from openmhd_gb300 import harris3d
 
