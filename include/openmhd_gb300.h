@@ -219,6 +219,11 @@ int omhd_probe_fp32_peak(double* gflops);
  * (the second and last by the device's IEEE division and square root);
  * synchronous, on the default stream */
 int omhd_probe_fastmath(const double* x_dev, long long n, double* out_dev);
+/* probe of the integer-pipe binary32 <-> binary64 conversions of the
+ * FP32-mixed kernels (no counterpart in the reference): for n device values,
+ * nd_dev[i] = narrow(xd_dev[i]) and wf_dev[i] = widen(xf_dev[i]); synchronous,
+ * on the default stream */
+int omhd_probe_convert(const double* xd_dev, float* nd_dev, const float* xf_dev, double* wf_dev, long long n);
 
 /* ======================================================================
  * Fused solver handle

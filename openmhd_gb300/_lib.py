@@ -98,6 +98,7 @@ SIGNATURES = [
     ("omhd_set_tma_staging", None, [I]),
     ("omhd_set_3d_pipeline", None, [I]),
     ("omhd_probe_fastmath", I, [P, C.c_longlong, P]),
+    ("omhd_probe_convert", I, [P, P, P, P, C.c_longlong]),
     ("omhd_solver_create", I, [C.POINTER(Config), C.POINTER(C.c_void_p)]),
     ("omhd_solver_destroy", I, [P]),
     ("omhd_solver_set_stream", I, [P, P]),

@@ -1,5 +1,6 @@
 // omhd_fastmath.h -- FP64 reciprocal and reciprocal square root by
-// Newton-Raphson from hardware approximations (device code).
+// Newton-Raphson from hardware approximations, and binary32 <-> binary64
+// conversions on the integer pipe (device code).
 #pragma once
 
 namespace omhd {
@@ -62,6 +63,47 @@ __device__ __forceinline__ double sqrt_nr(double x) {
   const double s = x * r;
   const double e = fma(-s, r, 1.0);
   return fma(s * e, fma(0.375, e, 0.5), s);
+}
+
+// ---------------------------------------------------------------------------
+// binary32 <-> binary64 conversions on the integer pipe.  GB300 executes the
+// F2F conversions on its FP64 pipe, one slot each like an FMA; the FP32-mixed
+// kernels convert every loaded primitive to binary32 and every face flux back,
+// which took a quarter of their FP64-pipe time.  These forms move the bits with
+// 8-15 integer instructions instead (IEEE 754 formats: binary32 = 1/8/23 bits,
+// bias 127; binary64 = 1/11/52 bits, bias 1023):
+//   widen_f32  : exact for normal floats, +-0, +-inf and NaN (payload kept);
+//                a subnormal float (|f| < 2^-126) becomes a signed zero.
+//   narrow_f64 : round to nearest, ties to even, as cvt.rn.f32.f64, for every
+//                argument of magnitude 2^-126 or more, with overflow to
+//                +-inf; a smaller argument gives a signed zero (no subnormal
+//                results); NaN stays NaN (quiet).
+// tests/test_gpu_convert.py checks both against IEEE conversions on the host,
+// bit for bit, over random bit patterns and every boundary of the formats.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double widen_f32(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned mag = u & 0x7fffffffu;
+  // rebias the exponent: + (1023 - 127) in the high word's exponent field, and
+  // twice that for inf/NaN so that exponent 255 lands on 2047
+  unsigned hi = (mag >> 3) + (mag >= 0x7f800000u ? 0x70000000u : 0x38000000u);
+  unsigned lo = u << 29;  // the three low mantissa bits
+  if (mag < 0x00800000u) hi = lo = 0u;
+  return __hiloint2double((int)(hi | (u & 0x80000000u)), (int)lo);
+}
+
+__device__ __forceinline__ float narrow_f64(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned ahi = hi & 0x7fffffffu;
+  // round the 64-bit magnitude at bit 29: add half an ulp of the result minus
+  // one, plus the kept lowest bit (ties go to even), then drop 29 bits
+  const unsigned long long a = ((unsigned long long)ahi << 32) | lo;
+  const unsigned long long r = a + (0x0fffffffull + ((lo >> 29) & 1u));
+  unsigned f = (unsigned)(r >> 29) - (896u << 23);  // rebias 1023 -> 127
+  f = ahi >= 0x47f00000u ? 0x7f800000u : f;         // |x| >= 2^128: inf (also inf/NaN inputs)
+  f = ahi < 0x38100000u ? 0u : f;                   // |x| < 2^-126: zero
+  f = a > 0x7ff0000000000000ull ? 0x7fc00000u : f;  // NaN
+  return __uint_as_float(f | (hi & 0x80000000u));
 }
 #endif
 

@@ -119,6 +119,29 @@ struct TileMem {
   int fxv, fxr, fyv;
 };
 
+// Scalars of one stage that each thread would otherwise derive itself (four
+// FP64 divisions per thread and tile, and for FP32 face arithmetic four
+// conversions): one thread computes them per CTA -- per work item in an
+// ensemble -- into shared memory, and the others read them after the next
+// CTA barrier.  Same expressions, so the same bits.
+template <class T>
+struct StageScalars {
+  double glmf;        // GLM damping factor of the step (glm_ss2.f90:27)
+  double dtx, dty;    // dtx_scale * dt / dx and / dy (rk.f90:22)
+  T ch, gam, r1, r2;  // GLM speed, gamma, 1/(gamma-1), gamma/(gamma-1) (flux_solver.f90:38-39)
+};
+template <class T>
+__device__ __forceinline__ void stage_scalars(const StageArgs& a, const StepState* st, StageScalars<T>& k) {
+  const double dt = st->dt, g = a.gamma;
+  k.glmf = st->glm_f;
+  k.dtx = a.dtx_scale * dt / a.dx;
+  k.dty = a.dtx_scale * dt / a.dy;
+  k.ch = T(st->ch);
+  k.gam = T(g);
+  k.r1 = T(1.0 / (g - 1.0));
+  k.r2 = T(g / (g - 1.0));
+}
+
 template <class T, class G>
 __device__ __forceinline__ TileMem<T> tile_mem_separate(unsigned char* smem_raw) {
   TileMem<T> m;
@@ -195,15 +218,15 @@ __device__ __forceinline__ void phase_load(const StageArgs& a, int bxi, int byi,
       const double pr = f1g * (u[b][EN] - 0.5 * (rv2 + B2));  // u2v.f90:27
       double ps = u[b][PS];
       if (a.stage == 1) ps = glmf * ps;
-      W[VX * PL + q] = T(vx);
-      W[VY * PL + q] = T(vy);
-      W[VZ * PL + q] = T(vz);
-      W[PR * PL + q] = T(pr);
-      W[RO * PL + q] = T(ro);
-      W[BX * PL + q] = T(bx);
-      W[BY * PL + q] = T(by);
-      W[BZ * PL + q] = T(bz);
-      W[PS * PL + q] = T(ps);
+      W[VX * PL + q] = to_face<T>(vx);
+      W[VY * PL + q] = to_face<T>(vy);
+      W[VZ * PL + q] = to_face<T>(vz);
+      W[PR * PL + q] = to_face<T>(pr);
+      W[RO * PL + q] = to_face<T>(ro);
+      W[BX * PL + q] = to_face<T>(bx);
+      W[BY * PL + q] = to_face<T>(by);
+      W[BZ * PL + q] = to_face<T>(bz);
+      W[PS * PL + q] = to_face<T>(ps);
       if (cx_in && cy_in && gi <= ix - 2 && gj <= jx - 2) {  // owner check, u2v.f90:36-45
         if (!gt0_<OMHD_FAST>(pr))
           raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, 0, 0, pr);
@@ -384,7 +407,7 @@ __device__ __forceinline__ constexpr int rot_y(int k) {
 // direction to whole warps: 18).
 template <class T, int FLUX, class G, int TAPE>
 __device__ __forceinline__ void phase_flux_rot(const StageArgs& a, int bxi, int byi, const TileMem<T>& m, int t,
-                                               int n, double chd) {
+                                               int n, const StageScalars<T>& ks) {
   constexpr int TX = G::TX, RX = G::RX;
   constexpr int NXS = G::NXS, NYS = G::NYS, NXF = G::NXF, NYF = G::NYF, XS = TX + 2, XF = TX + 1;
   constexpr int PL = RX * G::RY;
@@ -392,9 +415,7 @@ __device__ __forceinline__ void phase_flux_rot(const StageArgs& a, int bxi, int 
   const size_t N = (size_t)ix * jx;
   const int gi0 = 1 + bxi * TX, gj0 = 1 + byi * G::TY;
   const bool resist = a.eta_kind != OMHD_ETA_NONE;
-  const double gamma = a.gamma;
-  const T ch = T(chd), gam = T(gamma);
-  const T r1 = T(1.0 / (gamma - 1.0)), r2 = T(gamma / (gamma - 1.0));
+  const T ch = ks.ch, gam = ks.gam, r1 = ks.r1, r2 = ks.r2;
   const T* W = m.W;
   for (int q = t; q < NXF + NYF; q += n) {
     const bool xd = q < NXF;
@@ -433,13 +454,13 @@ __device__ __forceinline__ void phase_flux_rot(const StageArgs& a, int bxi, int 
     }
     double F[NV];  // back to the grid's component order
 #pragma unroll
-    for (int k = 0; k < NV; ++k) F[rot_y(k)] = xd ? double(Fo[rot_y(k)]) : double(Fo[k]);
+    for (int k = 0; k < NV; ++k) F[rot_y(k)] = xd ? to_f64<T>(Fo[rot_y(k)]) : to_f64<T>(Fo[k]);
     if (resist) {
       if (xd) {  // 2D_reconnection/flux_resistive.f90:266-283
         const int fx = fa, cy = fb, g = gi0 - 1 + fx, gj = gj0 + cy;
         if (g >= 0 && g <= ix - 2 && gj <= jx - 2) {
           const int o = (cy + 2) * RX + (fx + 1);  // region index of cell g
-          auto B = [&](int var, int dxo, int dyo) { return double(W[var * PL + o + dxo + dyo * RX]); };
+          auto B = [&](int var, int dxo, int dyo) { return to_f64<T>(W[var * PL + o + dxo + dyo * RX]); };
           const double odx = 1.0 / a.dx;
           const double eta_dx = eta_at(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gj], 0.0) * odx;
           const double JyS = -eta_dx * (B(BZ, 1, 0) - B(BZ, 0, 0));
@@ -453,7 +474,7 @@ __device__ __forceinline__ void phase_flux_rot(const StageArgs& a, int bxi, int 
         const int cx = fa, fy = fb, gi = gi0 + cx, g = gj0 - 1 + fy;
         if (g >= 0 && g <= jx - 2 && gi <= ix - 2) {
           const int o = (fy + 1) * RX + (cx + 2);  // region index of cell (gi, g)
-          auto B = [&](int var, int dxo, int dyo) { return double(W[var * PL + o + dxo + dyo * RX]); };
+          auto B = [&](int var, int dxo, int dyo) { return to_f64<T>(W[var * PL + o + dxo + dyo * RX]); };
           const double odx = 1.0 / a.dx;
           const double eta_dx = eta_at(a.eta_kind, a.xc[gi], a.yc[g] + 0.5 * a.dx, 0.0) * odx;
           const double JxS = eta_dx * (B(BZ, 0, 1) - B(BZ, 0, 0));
@@ -476,9 +497,9 @@ __device__ __forceinline__ void phase_flux_rot(const StageArgs& a, int bxi, int 
 // warps) and all y faces (items NXFP..NXFP+NYF-1)
 template <class T, int FLUX, class G, int TAPE>
 __device__ __forceinline__ void phase_flux(const StageArgs& a, int bxi, int byi, const TileMem<T>& m, int t, int n,
-                                           double chd) {
+                                           const StageScalars<T>& ks) {
   if constexpr (OMHD_FAST && sizeof(T) == 8) {
-    phase_flux_rot<T, FLUX, G, TAPE>(a, bxi, byi, m, t, n, chd);
+    phase_flux_rot<T, FLUX, G, TAPE>(a, bxi, byi, m, t, n, ks);
     return;
   }
   constexpr int TX = G::TX, RX = G::RX;
@@ -488,9 +509,7 @@ __device__ __forceinline__ void phase_flux(const StageArgs& a, int bxi, int byi,
   const size_t N = (size_t)ix * jx;
   const int gi0 = 1 + bxi * TX, gj0 = 1 + byi * G::TY;
   const bool resist = a.eta_kind != OMHD_ETA_NONE;
-  const double gamma = a.gamma;
-  const T ch = T(chd), gam = T(gamma);
-  const T r1 = T(1.0 / (gamma - 1.0)), r2 = T(gamma / (gamma - 1.0));
+  const T ch = ks.ch, gam = ks.gam, r1 = ks.r1, r2 = ks.r2;
   const T* W = m.W;
   constexpr int XF = TX + 1;
   for (int q = t; q < NXFP + NYF; q += n) {
@@ -517,19 +536,19 @@ __device__ __forceinline__ void phase_flux(const StageArgs& a, int bxi, int byi,
         const int g = gi0 - 1 + fx, gj = gj0 + cy;
         if (g >= 0 && g <= ix - 2 && gj <= jx - 2) {
           const int o = (cy + 2) * RX + (fx + 1);  // region index of cell g
-          auto B = [&](int var, int dxo, int dyo) { return double(W[var * PL + o + dxo + dyo * RX]); };
+          auto B = [&](int var, int dxo, int dyo) { return to_f64<T>(W[var * PL + o + dxo + dyo * RX]); };
           const double odx = 1.0 / a.dx;
           const double eta_dx = eta_at(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gj], 0.0) * odx;
           const double JyS = -eta_dx * (B(BZ, 1, 0) - B(BZ, 0, 0));
           const double JzS = eta_dx * ((B(BY, 1, 0) - B(BY, 0, 0)) -
                                        0.25 * (B(BX, 0, 1) + B(BX, 1, 1) - B(BX, 0, -1) - B(BX, 1, -1)));
-          Fo[EN] = T(double(Fo[EN]) + 0.5 * (JyS * (B(BZ, 0, 0) + B(BZ, 1, 0)) - JzS * (B(BY, 0, 0) + B(BY, 1, 0))));
-          Fo[BY] = T(double(Fo[BY]) - JzS);
-          Fo[BZ] = T(double(Fo[BZ]) + JyS);
+          Fo[EN] = to_face<T>(to_f64<T>(Fo[EN]) + 0.5 * (JyS * (B(BZ, 0, 0) + B(BZ, 1, 0)) - JzS * (B(BY, 0, 0) + B(BY, 1, 0))));
+          Fo[BY] = to_face<T>(to_f64<T>(Fo[BY]) - JzS);
+          Fo[BZ] = to_face<T>(to_f64<T>(Fo[BZ]) + JyS);
         }
       }
 #pragma unroll
-      for (int v = 0; v < NV; ++v) m.FX[v * m.fxv + cy * m.fxr + fx] = double(Fo[v]);
+      for (int v = 0; v < NV; ++v) m.FX[v * m.fxv + cy * m.fxr + fx] = to_f64<T>(Fo[v]);
     } else {
       const int qq = q - NXFP;
       const int cx = qq % TX, fy = qq / TX;
@@ -553,19 +572,19 @@ __device__ __forceinline__ void phase_flux(const StageArgs& a, int bxi, int byi,
         const int gi = gi0 + cx, g = gj0 - 1 + fy;
         if (g >= 0 && g <= jx - 2 && gi <= ix - 2) {
           const int o = (fy + 1) * RX + (cx + 2);  // region index of cell (gi, g)
-          auto B = [&](int var, int dxo, int dyo) { return double(W[var * PL + o + dxo + dyo * RX]); };
+          auto B = [&](int var, int dxo, int dyo) { return to_f64<T>(W[var * PL + o + dxo + dyo * RX]); };
           const double odx = 1.0 / a.dx;
           const double eta_dx = eta_at(a.eta_kind, a.xc[gi], a.yc[g] + 0.5 * a.dx, 0.0) * odx;
           const double JxS = eta_dx * (B(BZ, 0, 1) - B(BZ, 0, 0));
           const double JzS = eta_dx * (0.25 * (B(BY, 1, 1) + B(BY, 1, 0) - B(BY, -1, 1) - B(BY, -1, 0)) -
                                        (B(BX, 0, 1) - B(BX, 0, 0)));
-          Fo[EN] = T(double(Fo[EN]) + 0.5 * (JzS * (B(BX, 0, 0) + B(BX, 0, 1)) - JxS * (B(BZ, 0, 0) + B(BZ, 0, 1))));
-          Fo[BX] = T(double(Fo[BX]) + JzS);
-          Fo[BZ] = T(double(Fo[BZ]) - JxS);
+          Fo[EN] = to_face<T>(to_f64<T>(Fo[EN]) + 0.5 * (JzS * (B(BX, 0, 0) + B(BX, 0, 1)) - JxS * (B(BZ, 0, 0) + B(BZ, 0, 1))));
+          Fo[BX] = to_face<T>(to_f64<T>(Fo[BX]) + JzS);
+          Fo[BZ] = to_face<T>(to_f64<T>(Fo[BZ]) - JxS);
         }
       }
 #pragma unroll
-      for (int v = 0; v < NV; ++v) m.FY[v * m.fyv + fy * TX + cx] = double(Fo[v]);
+      for (int v = 0; v < NV; ++v) m.FY[v * m.fyv + fy * TX + cx] = to_f64<T>(Fo[v]);
     }
   }
 }
@@ -574,7 +593,7 @@ __device__ __forceinline__ void phase_flux(const StageArgs& a, int bxi, int byi,
 // returns this thread's largest CFL speed (stage 2) or 0
 template <class T, class G>
 __device__ __forceinline__ double phase_update(const StageArgs& a, int bxi, int byi, const TileMem<T>& m, int t,
-                                               int n, double dt, double glmf) {
+                                               int n, const StageScalars<T>& ks) {
   constexpr int TX = G::TX, TY = G::TY;
   const int ix = a.ix, jx = a.jx;
   const size_t N = (size_t)ix * jx;
@@ -589,7 +608,7 @@ __device__ __forceinline__ double phase_update(const StageArgs& a, int bxi, int 
   double* const Uhost = a.Uhost;
   const double* const Ubase = a.Ubase;
   const double* const U1 = a.U1;
-  const double dtx = a.dtx_scale * dt / a.dx, dty = a.dtx_scale * dt / a.dy;
+  const double dtx = ks.dtx, dty = ks.dty, glmf = ks.glmf;
   const bool iso = a.iso, rk2 = a.stage == 1 || a.time_type == OMHD_TIME_RK2, stage2 = a.stage == 2;
   int flip[4];
 #pragma unroll
@@ -667,10 +686,10 @@ __device__ __forceinline__ double phase_update(const StageArgs& a, int bxi, int 
 // updated cells (stage 2) or 0.  Three or four CTA-wide barriers.
 template <class T, int FLUX, class G, int TAPE = tape::kNone>
 __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int byi, unsigned char* smem_raw,
-                                               double dt, double chd, double glmf) {
+                                               const StageScalars<T>& ks) {
   const TileMem<T> m = tile_mem_separate<T, G>(smem_raw);
   const int tid = threadIdx.x;
-  phase_load<T, G>(a, bxi, byi, m, tid, G::NT, glmf);
+  phase_load<T, G>(a, bxi, byi, m, tid, G::NT, ks.glmf);
   __syncthreads();
   phase_recon<T, G, TAPE>(a, bxi, byi, m, tid, G::NT);
   __syncthreads();
@@ -678,9 +697,9 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
     phase_walls<T, G>(a, bxi, byi, m, tid, G::NT);
     __syncthreads();
   }
-  phase_flux<T, FLUX, G, TAPE>(a, bxi, byi, m, tid, G::NT, chd);
+  phase_flux<T, FLUX, G, TAPE>(a, bxi, byi, m, tid, G::NT, ks);
   __syncthreads();
-  return phase_update<T, G>(a, bxi, byi, m, tid, G::NT, dt, glmf);
+  return phase_update<T, G>(a, bxi, byi, m, tid, G::NT, ks);
 }
 
 // one CTA per tile of one grid
@@ -690,14 +709,17 @@ __global__ void __launch_bounds__(GeoFor<T>::type::NT, sizeof(T) == 4 ? 2 : 1) k
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red32[32];
   __shared__ int skip;
+  __shared__ StageScalars<T> ks;
   StepState* st = a.st;
   // one thread decides, so that the whole CTA leaves together (the error word
   // may be set by another CTA while this one starts)
-  if (threadIdx.x == 0) skip = st->done || *(volatile int*)&a.err->code;
+  if (threadIdx.x == 0) {
+    skip = st->done || *(volatile int*)&a.err->code;
+    stage_scalars<T>(a, st, ks);
+  }
   __syncthreads();
   if (skip) return;
-  const double vcell = stage2d_tile<T, FLUX, G, TAPE>(a, blockIdx.x, blockIdx.y, smem_raw, st->dt, st->ch,
-                                                               st->glm_f);
+  const double vcell = stage2d_tile<T, FLUX, G, TAPE>(a, blockIdx.x, blockIdx.y, smem_raw, ks);
   if (a.stage == 2) {
     const double bm = block_max_pos(vcell, red32);
     StepConsts sc{a.cfl, a.dmin, a.dx, a.eta_kind};
@@ -769,11 +791,15 @@ __global__ void __launch_bounds__(NPW * 32 + PipeGeo::NT, 1)
   __shared__ double red32[32];
   __shared__ __align__(8) uint64_t tma_bar;
   __shared__ int skip;
+  __shared__ StageScalars<double> ks;
   StepState* st = a.st;
-  if (threadIdx.x == 0) skip = st->done || *(volatile int*)&a.err->code;
+  if (threadIdx.x == 0) {
+    skip = st->done || *(volatile int*)&a.err->code;
+    stage_scalars<double>(a, st, ks);
+  }
   __syncthreads();
   if (skip) return;
-  const double dt = st->dt, chd = st->ch, glmf = st->glm_f;
+  const double glmf = ks.glmf;
   const int ntx = (a.ix - 2 + G::TX - 1) / G::TX;
   const int ntiles = ntx * ((a.jx - 2 + G::TY - 1) / G::TY);
   const bool walls = a.bc_kind[0] != OMHD_BC_PERIODIC || a.bc_kind[2] != OMHD_BC_PERIODIC;
@@ -841,9 +867,9 @@ __global__ void __launch_bounds__(NPW * 32 + PipeGeo::NT, 1)
       const int b = i & 1;
       const TileMem<double> m = pipe_mem(smem_raw, b);
       named_bar_sync(kPipeBarFull + b, NTOT);
-      phase_flux<double, FLUX, G, TAPE>(a, w % ntx, w / ntx, m, t, NC, chd);
+      phase_flux<double, FLUX, G, TAPE>(a, w % ntx, w / ntx, m, t, NC, ks);
       named_bar_sync(kPipeBarCons, NC);
-      const double v = phase_update<double, G>(a, w % ntx, w / ntx, m, t, NC, dt, glmf);
+      const double v = phase_update<double, G>(a, w % ntx, w / ntx, m, t, NC, ks);
       vmax = lt_<double, OMHD_FAST>(vmax, v) ? v : vmax;
       if (i + 2 < nmine) {  // the producers refill buffer b for tile i+2
         __threadfence_block();
@@ -901,6 +927,7 @@ __global__ void __launch_bounds__(G::NT, sizeof(T) == 4 ? 2 : 1) k_batch2d(const
   __shared__ double red32[32];
   __shared__ unsigned int is_last;
   __shared__ int skip_s, w_s;
+  __shared__ StageScalars<T> ks;
   for (;;) {
     if (threadIdx.x == 0) w_s = atomicAdd(queue, 1);
     __syncthreads();
@@ -919,11 +946,14 @@ __global__ void __launch_bounds__(G::NT, sizeof(T) == 4 ? 2 : 1) k_batch2d(const
     const int local = w - tile_start[lo];
     const int ntx = (a.ix - 2 + G::TX - 1) / G::TX;
     const int ntiles = ntx * ((a.jx - 2 + G::TY - 1) / G::TY);
-    if (threadIdx.x == 0) skip_s = st->done || *(volatile int*)&a.err->code;
+    if (threadIdx.x == 0) {
+      skip_s = st->done || *(volatile int*)&a.err->code;
+      stage_scalars<T>(a, st, ks);
+    }
     __syncthreads();
     const bool skip = skip_s;  // uniform over the CTA
     double vcell = 0.0;
-    if (!skip) vcell = stage2d_tile<T, FLUX, G>(a, local % ntx, local / ntx, smem_raw, st->dt, st->ch, st->glm_f);
+    if (!skip) vcell = stage2d_tile<T, FLUX, G>(a, local % ntx, local / ntx, smem_raw, ks);
     if (!skip && a.stage == 2) {
       const double bm = block_max_pos(vcell, red32);
       if (threadIdx.x == 0) {

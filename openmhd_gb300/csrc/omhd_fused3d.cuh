@@ -96,15 +96,15 @@ __device__ __forceinline__ void load_plane(const StageArgs& a, T* W, int slot, i
     const double pr = f1g * (U[EN * N + c] - 0.5 * (rv2 + B2));
     double ps = U[PS * N + c];
     if (a.stage == 1) ps = glmf * ps;
-    Ws[VX * PL + q] = T(vx);
-    Ws[VY * PL + q] = T(vy);
-    Ws[VZ * PL + q] = T(vz);
-    Ws[PR * PL + q] = T(pr);
-    Ws[RO * PL + q] = T(ro);
-    Ws[BX * PL + q] = T(bx);
-    Ws[BY * PL + q] = T(by);
-    Ws[BZ * PL + q] = T(bz);
-    Ws[PS * PL + q] = T(ps);
+    Ws[VX * PL + q] = to_face<T>(vx);
+    Ws[VY * PL + q] = to_face<T>(vy);
+    Ws[VZ * PL + q] = to_face<T>(vz);
+    Ws[PR * PL + q] = to_face<T>(pr);
+    Ws[RO * PL + q] = to_face<T>(ro);
+    Ws[BX * PL + q] = to_face<T>(bx);
+    Ws[BY * PL + q] = to_face<T>(by);
+    Ws[BZ * PL + q] = to_face<T>(bz);
+    Ws[PS * PL + q] = to_face<T>(ps);
     if (own_plane && cx_in && cy_in && gi <= ix - 2 && gj <= jx - 2) {  // u2v.f90:36-45, owner check
       if (pr <= 0)
         raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, gk + 1, 0, pr);
@@ -199,10 +199,10 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
     }
     riemann_flux<T, 3, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) Fzp[v] = double(Fo[v]);
+    for (int v = 0; v < NV; ++v) Fzp[v] = to_f64<T>(Fo[v]);
     if (resist && own) {  // z face k0-1/2 (flux_resistive.cuf:121-135)
       const int k = k0 - 1;
-      auto B = [&](int var, int dxo, int dyo, int dzo) { return double(Wv(k + dzo, var, oc + dxo + dyo * RX)); };
+      auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, oc + dxo + dyo * RX)); };
       const double eta_dx = sep_eta ? harris_eta_dx(ex_c[tx + 1], ez_f[0], inv_dx)
                                     : eta3(a.eta_kind, a.xc[gi], a.yc[gj], a.zc[k] + 0.5 * a.dx) / a.dx;
       const double JyS = (B(BX, 0, 0, 1) - B(BX, 0, 0, 0)) -
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
       Fzp[BY] = Fzp[BY] + eta_dx * JxS;
       if (sizeof(T) == 4) {  // keep the face value the mixed build would round to
 #pragma unroll
-        for (int v = 0; v < NV; ++v) Fzp[v] = double(T(Fzp[v]));
+        for (int v = 0; v < NV; ++v) Fzp[v] = to_f64<T>(to_face<T>(Fzp[v]));
       }
     }
   }
@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
       // positivity of the current plane's own cells (u2v.f90:36-45); plane k0
       // was checked at load time in the prologue
       if (own) {
-        const double ro = double(Wv(k, RO, oc)), pr = double(Wv(k, PR, oc));
+        const double ro = to_f64<T>(Wv(k, RO, oc)), pr = to_f64<T>(Wv(k, PR, oc));
         if (pr <= 0)
           raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, k + 1, 0, pr);
         else if (ro <= 0)
@@ -279,16 +279,16 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
         const int g = gi0 - 1 + fx, gjj = gj0 + cy;
         if (g >= 0 && g <= ix - 2 && gjj <= jx - 2) {
           const int o = (cy + 2) * RX + (fx + 1);
-          auto B = [&](int var, int dxo, int dyo, int dzo) { return double(Wv(k + dzo, var, o + dxo + dyo * RX)); };
+          auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, o + dxo + dyo * RX)); };
           const double eta_dx = sep_eta ? harris_eta_dx(ex_f[fx], ez_c[k - k0 + 1], inv_dx)
                                         : eta3(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gjj], a.zc[k]) / a.dx;
           const double JyS = -(B(BZ, 1, 0, 0) - B(BZ, 0, 0, 0)) +
                              0.25 * (B(BX, 0, 0, 1) + B(BX, 1, 0, 1) - B(BX, 0, 0, -1) - B(BX, 1, 0, -1));
           const double JzS = (B(BY, 1, 0, 0) - B(BY, 0, 0, 0)) -
                              0.25 * (B(BX, 0, 1, 0) + B(BX, 1, 1, 0) - B(BX, 0, -1, 0) - B(BX, 1, -1, 0));
-          Fo[EN] = T(double(Fo[EN]) + 0.5 * eta_dx * (JyS * (B(BZ, 0, 0, 0) + B(BZ, 1, 0, 0)) - JzS * (B(BY, 0, 0, 0) + B(BY, 1, 0, 0))));
-          Fo[BY] = T(double(Fo[BY]) - eta_dx * JzS);
-          Fo[BZ] = T(double(Fo[BZ]) + eta_dx * JyS);
+          Fo[EN] = to_face<T>(to_f64<T>(Fo[EN]) + 0.5 * eta_dx * (JyS * (B(BZ, 0, 0, 0) + B(BZ, 1, 0, 0)) - JzS * (B(BY, 0, 0, 0) + B(BY, 1, 0, 0))));
+          Fo[BY] = to_face<T>(to_f64<T>(Fo[BY]) - eta_dx * JzS);
+          Fo[BZ] = to_face<T>(to_f64<T>(Fo[BZ]) + eta_dx * JyS);
         }
       }
 #pragma unroll
@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
     double acc[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v)
-      acc[v] = double(FB[v * SFLUX + ty * XF + tx]) - double(FB[v * SFLUX + ty * XF + tx + 1]);
+      acc[v] = to_f64<T>(FB[v * SFLUX + ty * XF + tx]) - to_f64<T>(FB[v * SFLUX + ty * XF + tx + 1]);
     // no barrier here: the y reconstruction writes only SL/SR (last read by the
     // x fluxes, before the barrier above), and FB is next written by the y
     // fluxes, after the barrier that follows the y reconstruction
@@ -345,16 +345,16 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
         const int gii = gi0 + cx, g = gj0 - 1 + fy;
         if (g >= 0 && g <= jx - 2 && gii <= ix - 2) {
           const int o = (fy + 1) * RX + (cx + 2);
-          auto B = [&](int var, int dxo, int dyo, int dzo) { return double(Wv(k + dzo, var, o + dxo + dyo * RX)); };
+          auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, o + dxo + dyo * RX)); };
           const double eta_dx = sep_eta ? harris_eta_dx(ex_c[cx + 1], ez_c[k - k0 + 1], inv_dx)
                                         : eta3(a.eta_kind, a.xc[gii], a.yc[g] + 0.5 * a.dx, a.zc[k]) / a.dx;
           const double JxS = (B(BZ, 0, 1, 0) - B(BZ, 0, 0, 0)) -
                              0.25 * (B(BY, 0, 0, 1) + B(BY, 0, 1, 1) - B(BY, 0, 0, -1) - B(BY, 0, 1, -1));
           const double JzS = -(B(BX, 0, 1, 0) - B(BX, 0, 0, 0)) +
                              0.25 * (B(BY, 1, 0, 0) + B(BY, 1, 1, 0) - B(BY, -1, 0, 0) - B(BY, -1, 1, 0));
-          Fo[EN] = T(double(Fo[EN]) + 0.5 * eta_dx * (JzS * (B(BX, 0, 0, 0) + B(BX, 0, 1, 0)) - JxS * (B(BZ, 0, 0, 0) + B(BZ, 0, 1, 0))));
-          Fo[BX] = T(double(Fo[BX]) + eta_dx * JzS);
-          Fo[BZ] = T(double(Fo[BZ]) - eta_dx * JxS);
+          Fo[EN] = to_face<T>(to_f64<T>(Fo[EN]) + 0.5 * eta_dx * (JzS * (B(BX, 0, 0, 0) + B(BX, 0, 1, 0)) - JxS * (B(BZ, 0, 0, 0) + B(BZ, 0, 1, 0))));
+          Fo[BX] = to_face<T>(to_f64<T>(Fo[BX]) + eta_dx * JzS);
+          Fo[BZ] = to_face<T>(to_f64<T>(Fo[BZ]) - eta_dx * JxS);
         }
       }
 #pragma unroll
@@ -364,8 +364,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
     double gm[NV], gp[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      gm[v] = double(FB[v * SFLUX + ty * TX + tx]);
-      gp[v] = double(FB[v * SFLUX + (ty + 1) * TX + tx]);
+      gm[v] = to_f64<T>(FB[v * SFLUX + ty * TX + tx]);
+      gp[v] = to_f64<T>(FB[v * SFLUX + (ty + 1) * TX + tx]);
     }
 
     // ---- z face k+1/2 in registers ----
@@ -387,9 +387,9 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
       }
       riemann_flux<T, 3, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
 #pragma unroll
-      for (int v = 0; v < NV; ++v) Fzc[v] = double(Fo[v]);
+      for (int v = 0; v < NV; ++v) Fzc[v] = to_f64<T>(Fo[v]);
       if (resist && own) {  // flux_resistive.cuf:121-135
-        auto B = [&](int var, int dxo, int dyo, int dzo) { return double(Wv(k + dzo, var, oc + dxo + dyo * RX)); };
+        auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, oc + dxo + dyo * RX)); };
         const double eta_dx = sep_eta ? harris_eta_dx(ex_c[tx + 1], ez_f[k - k0 + 1], inv_dx)
                                       : eta3(a.eta_kind, a.xc[gi], a.yc[gj], a.zc[k] + 0.5 * a.dx) / a.dx;
         const double JyS = (B(BX, 0, 0, 1) - B(BX, 0, 0, 0)) -
@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
         Fzc[BY] = Fzc[BY] + eta_dx * JxS;
         if (sizeof(T) == 4) {
 #pragma unroll
-          for (int v = 0; v < NV; ++v) Fzc[v] = double(T(Fzc[v]));
+          for (int v = 0; v < NV; ++v) Fzc[v] = to_f64<T>(to_face<T>(Fzc[v]));
         }
       }
     }

@@ -96,6 +96,24 @@ __device__ __forceinline__ T divr_(T a, T b, T rb) {
   return a / b;
 }
 
+// primitive (FP64) -> the face arithmetic's type T, and face flux -> FP64: the
+// FP32-mixed kernels convert on the integer pipe (omhd_fastmath.h), the FP64
+// kernels pass the value through
+template <class T>
+__device__ __forceinline__ T to_face(double x) {
+  if constexpr (sizeof(T) == 4)
+    return narrow_f64(x);
+  else
+    return x;
+}
+template <class T>
+__device__ __forceinline__ double to_f64(T x) {
+  if constexpr (sizeof(T) == 4)
+    return widen_f32(x);
+  else
+    return x;
+}
+
 enum { LM_FLAT = 0, LM_MINMOD = 1, LM_MC = 2, LM_VANLEER = 3, LM_KOREN = 4 };
 enum { FX_LLF = 0, FX_HLL = 1, FX_HLLC = 2, FX_HLLD = 3, FX_LHLLD = 4 };
 

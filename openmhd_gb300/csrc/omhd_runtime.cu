@@ -189,6 +189,14 @@ __global__ void k_fastmath_probe(const double* __restrict__ x, long long n, doub
   }
 }
 
+__global__ void k_convert_probe(const double* __restrict__ xd, float* __restrict__ nd, const float* __restrict__ xf,
+                                double* __restrict__ wf, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    nd[i] = narrow_f64(xd[i]);
+    wf[i] = widen_f32(xf[i]);
+  }
+}
+
 static std::atomic<int> g_tma_on{1};
 bool tma_staging_enabled() { return g_tma_on.load(std::memory_order_relaxed) != 0; }
 static std::atomic<int> g_pipe3d_on{1};
@@ -245,6 +253,25 @@ int omhd_probe_fastmath(const double* x, long long n, double* out) {
   k_fastmath_probe<<<(unsigned)blocks, 256>>>(x, n, out);
   if (cuda_status(cudaGetLastError(), "fast-math probe launch")) return OMHD_CUDA_ERR;
   return cuda_status(cudaDeviceSynchronize(), "fast-math probe");
+}
+
+int omhd_probe_convert(const double* xd, float* nd, const float* xf, double* wf, long long n) {
+  if (!xd || !nd || !xf || !wf || n < 0) return OMHD_BAD_ARG;
+  if (n == 0) return OMHD_OK;
+  const void* ptrs[4] = {xd, nd, xf, wf};
+  for (const void* p : ptrs) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess || at.type != cudaMemoryTypeDevice) {
+      cudaGetLastError();
+      set_host_error(OMHD_BAD_ARG, 0, 0, 0, 0.0, "conversion probe: all four arrays must be device memory");
+      return OMHD_BAD_ARG;
+    }
+  }
+  long long blocks = (n + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  k_convert_probe<<<(unsigned)blocks, 256>>>(xd, nd, xf, wf, n);
+  if (cuda_status(cudaGetLastError(), "conversion probe launch")) return OMHD_CUDA_ERR;
+  return cuda_status(cudaDeviceSynchronize(), "conversion probe");
 }
 
 int omhd_probe_fp64_peak(double* gflops) {
