@@ -581,6 +581,7 @@ def run_batched(args, fp64_peak: float = float("nan"), fp32_peak: float = float(
             "cells": ens.cells, "precision": "mixed", "tile_kind": kind, "ctas_per_sm": cps,
             "tile": ["32x8", "32x4", "16x16", "64x4"][kind], "ms_per_step": 1e3 * t / args.steps,
             "steps_compared": total_steps, "max_member_scaled_l1_vs_fp64": max(errs),
+            "worst_member": int(np.argmax(errs)),
             "median_member_scaled_l1_vs_fp64": float(np.median(errs)),
             "dt_range": [min(x.dt for x in infos), max(x.dt for x in infos)]}
 
@@ -873,8 +874,48 @@ def run_accuracy(args):
                                                                     ("fp64_parity", "fp64"))
         res["accuracy"]["control_harris3d_fp64_vs_fp64_parity"] = curve(
             h3, min(args.accuracy_steps_3d, 300), sorted({10, 100, 300}), ("fp64_parity", "fp64"))
+    res["accuracy"]["ensemble_worst_members"] = _ensemble_worst_members(curve, args.accuracy_control)
     print(json.dumps(res), flush=True)
     return 0
+
+
+def _ensemble_worst_members(curve, control: bool, nworst: int = 3):
+    """The batched configuration's members with the largest FP32-mixed error
+    against FP64 after its 500 steps (both ensembles in one batched launch per
+    stage, as the bench's batched leg runs them), then each of those members
+    alone: its error curve, and with control=True the same member in FP64
+    against FP64 without multiply-add contraction (round-off growth)."""
+    import numpy as np
+    import torch
+
+    from openmhd_gb300.ensemble import Ensemble, batched_problem_set
+
+    cfgs, models = batched_problem_set(128, seed=0, precision="mixed")
+    cfg64, _ = batched_problem_set(128, seed=0, precision="fp64")
+    mx = Ensemble(cfgs).init_models(models)
+    r64 = Ensemble(cfg64).init_models(models)
+    mx.step(BATCH_STEPS)
+    r64.step(BATCH_STEPS)
+    mx.sync()
+    r64.sync()
+    errs = [_errors(mx.member_state(i)[:, 1:-1, 1:-1], r64.member_state(i)[:, 1:-1, 1:-1])["max_scaled_l1"]
+            for i in range(len(cfgs))]
+    del mx, r64
+    torch.cuda.empty_cache()
+    out = []
+    marks = sorted({10, 100, BATCH_STEPS})
+    for i in [int(k) for k in np.argsort(errs)[::-1][:nworst]]:
+        make = lambda p, i=i: (batched_problem_set(128, seed=0, precision=p)[0][i], models[i])  # noqa: E731
+        c = cfgs[i]
+        m = models[i]
+        rec = {"member": i, "grid": [c.ix - 2, c.jx - 2],
+               "model": ["orszag_tang", "kelvin_helmholtz", "harris"][m.kind],
+               "model_params": {"amp": m.amp, "bx0": m.bx0, "phase_x": m.phase_x, "phase_y": m.phase_y},
+               "ensemble_max_scaled_l1": errs[i], "mixed_vs_fp64": curve(make, BATCH_STEPS, marks)}
+        if control:
+            rec["control_fp64_vs_fp64_parity"] = curve(make, BATCH_STEPS, marks, ("fp64_parity", "fp64"))
+        out.append(rec)
+    return out
 
 
 def _fp64_peak_gflops(lib) -> float:
@@ -902,10 +943,13 @@ def run_profile(args):
 
     from openmhd_gb300 import Solver, harris3d, kelvin_helmholtz
 
-    if args.one_role_3d:
+    if args.one_role_3d or args.one_role_2d:
         from openmhd_gb300 import _lib
 
-        _lib.load().omhd_set_3d_pipeline(0)
+        if args.one_role_3d:
+            _lib.load().omhd_set_3d_pipeline(0)
+        if args.one_role_2d:
+            _lib.load().omhd_set_2d_pipeline(0)
     if args.nz:
         cfg, model = harris3d(args.nx, args.ny, args.nz, precision=args.precision)
     else:
@@ -1014,6 +1058,8 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_parity", "mixed"])
     ap.add_argument("--one-role-3d", action="store_true",
                     help="with --profile: the one-role FP64 3D stage kernel instead of the warp-specialised one")
+    ap.add_argument("--one-role-2d", action="store_true",
+                    help="with --profile: the one-role 2D stage kernels instead of the warp-specialised ones")
     ap.add_argument("--accuracy", action="store_true",
                     help="long-run error of the FP32-mixed path against FP64 (KH 2D and Harris 3D)")
     ap.add_argument("--accuracy-steps", type=int, default=2000)

@@ -210,6 +210,11 @@ void omhd_set_tma_staging(int enable);
  * kernel (same scheme; results agree to rounding), for comparisons.
  * Library-global: set it before stepping, from one thread. */
 void omhd_set_3d_pipeline(int enable);
+/* The warp-specialised FP64 2D stage kernel (HLLD with minmod or MC, no
+ * resistivity; no counterpart in the reference): on by default; 0 selects the
+ * one-role 2D kernel (same scheme; results agree to rounding), for
+ * comparisons.  Library-global: set it before stepping, from one thread. */
+void omhd_set_2d_pipeline(int enable);
 /* measured FP32 FMA throughput of the current GPU in GFLOP/s (the FP32 roofline
  * denominator of the mixed-precision kernels; no counterpart in the reference) */
 int omhd_probe_fp32_peak(double* gflops);

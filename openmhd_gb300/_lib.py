@@ -97,6 +97,7 @@ SIGNATURES = [
     ("omhd_probe_fp32_peak", I, [c_double_p]),
     ("omhd_set_tma_staging", None, [I]),
     ("omhd_set_3d_pipeline", None, [I]),
+    ("omhd_set_2d_pipeline", None, [I]),
     ("omhd_probe_fastmath", I, [P, C.c_longlong, P]),
     ("omhd_probe_convert", I, [P, P, P, P, C.c_longlong]),
     ("omhd_solver_create", I, [C.POINTER(Config), C.POINTER(C.c_void_p)]),

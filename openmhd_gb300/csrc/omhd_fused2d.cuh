@@ -172,6 +172,7 @@ __device__ __forceinline__ void phase_load(const StageArgs& a, int bxi, int byi,
   const bool perx = a.bc_kind[0] == OMHD_BC_PERIODIC, pery = a.bc_kind[2] == OMHD_BC_PERIODIC;
   const bool resist = a.eta_kind != OMHD_ETA_NONE;
   const double f1g = a.gamma - 1;  // u2v.f90:11
+  const float f1g32 = sizeof(T) == 4 ? narrow_f64(f1g) : 0.0f;
   T* W = m.W;
   // FP64: two cells per pass, both cells' loads issued before either is
   // converted, so their global-memory latencies overlap; FP32-mixed (two CTAs
@@ -207,31 +208,17 @@ __device__ __forceinline__ void phase_load(const StageArgs& a, int bxi, int byi,
       const int rx = q % RX, ry = q / RX;
       const bool cx_in = rx >= 2 && rx < TX + 2, cy_in = ry >= 2 && ry < TY + 2;
       const int gi = gi0 - 2 + rx, gj = gj0 - 2 + ry;
-      const double ro = u[b][RO];
-      const double mx = u[b][MX], my = u[b][MY], mz = u[b][MZ];
-      const double iro = rcp_<double, OMHD_FAST>(ro);  // one reciprocal for the three velocities
-      const double vx = divr_<double, OMHD_FAST>(mx, ro, iro), vy = divr_<double, OMHD_FAST>(my, ro, iro),
-                   vz = divr_<double, OMHD_FAST>(mz, ro, iro);  // u2v.f90:24
-      const double rv2 = vx * mx + vy * my + vz * mz;
-      const double bx = u[b][BX], by = u[b][BY], bz = u[b][BZ];
-      const double B2 = bx * bx + by * by + bz * bz;
-      const double pr = f1g * (u[b][EN] - 0.5 * (rv2 + B2));  // u2v.f90:27
       double ps = u[b][PS];
       if (a.stage == 1) ps = glmf * ps;
-      W[VX * PL + q] = to_face<T>(vx);
-      W[VY * PL + q] = to_face<T>(vy);
-      W[VZ * PL + q] = to_face<T>(vz);
-      W[PR * PL + q] = to_face<T>(pr);
-      W[RO * PL + q] = to_face<T>(ro);
-      W[BX * PL + q] = to_face<T>(bx);
-      W[BY * PL + q] = to_face<T>(by);
-      W[BZ * PL + q] = to_face<T>(bz);
-      W[PS * PL + q] = to_face<T>(ps);
+      T w[NV], pr, ro;
+      u2v_cell<T, OMHD_FAST>(u[b], f1g, f1g32, ps, w, pr, ro);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) W[v * PL + q] = w[v];
       if (cx_in && cy_in && gi <= ix - 2 && gj <= jx - 2) {  // owner check, u2v.f90:36-45
-        if (!gt0_<OMHD_FAST>(pr))
-          raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, 0, 0, pr);
-        else if (!gt0_<OMHD_FAST>(ro))
-          raise_error(a.err, OMHD_NEG_DENSITY, gi + 1, gj + 1, 0, 0, ro);
+        if (!pos_<T, OMHD_FAST>(pr))
+          raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, 0, 0, to_f64<T>(pr));
+        else if (!pos_<T, OMHD_FAST>(ro))
+          raise_error(a.err, OMHD_NEG_DENSITY, gi + 1, gj + 1, 0, 0, to_f64<T>(ro));
       }
     }
   }

@@ -13,7 +13,8 @@ int launch_stage2d_fp64(const StageArgs& a, cudaStream_t s) {
     StageArgs b = a;
     b.tlim = nullptr;
     b.tface = nullptr;
-    if (a.eta_kind == OMHD_ETA_NONE) return v_fp64::launch_pipe<FX_HLLD, tape::kRecord>(b, s);
+    if (a.eta_kind == OMHD_ETA_NONE && pipe2d_enabled())
+      return v_fp64::launch_pipe<FX_HLLD, tape::kRecord>(b, s);
     return v_fp64::launch_one<double, FX_HLLD, tape::kRecord>(b, s);
   }
   return v_fp64::launch_variant<double>(a, s);

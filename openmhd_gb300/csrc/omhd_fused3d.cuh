@@ -74,6 +74,7 @@ __device__ __forceinline__ void load_plane(const StageArgs& a, T* W, int slot, i
   const int ix = a.ix, jx = a.jx, kx = a.kx;
   const size_t N = (size_t)ix * jx * kx;
   const double f1g = a.gamma - 1;
+  const float f1g32 = sizeof(T) == 4 ? narrow_f64(f1g) : 0.0f;
   const int mk = map_idx(gk, kx, perz);
   T* Ws = W + (size_t)slot * NV * PL;
   for (int q = threadIdx.x; q < PL; q += NT) {
@@ -85,31 +86,20 @@ __device__ __forceinline__ void load_plane(const StageArgs& a, T* W, int slot, i
     const int gi = gi0 - 2 + rx, gj = gj0 - 2 + ry;
     const size_t c = (size_t)map_idx(gi, ix, perx) + (size_t)ix * ((size_t)map_idx(gj, jx, pery) + (size_t)jx * mk);
     const double* U = a.Uin;
-    const double ro = U[RO * N + c];
-    const double mx = U[MX * N + c], my = U[MY * N + c], mz = U[MZ * N + c];
-    const double iro = rcp_<double, OMHD_FAST>(ro);  // one reciprocal for the three velocities
-    const double vx = divr_<double, OMHD_FAST>(mx, ro, iro), vy = divr_<double, OMHD_FAST>(my, ro, iro),
-                 vz = divr_<double, OMHD_FAST>(mz, ro, iro);  // 3D_basic/u2v.f90:24
-    const double rv2 = vx * mx + vy * my + vz * mz;
-    const double bx = U[BX * N + c], by = U[BY * N + c], bz = U[BZ * N + c];
-    const double B2 = bx * bx + by * by + bz * bz;
-    const double pr = f1g * (U[EN * N + c] - 0.5 * (rv2 + B2));
-    double ps = U[PS * N + c];
+    double u[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) u[v] = U[v * N + c];
+    double ps = u[PS];
     if (a.stage == 1) ps = glmf * ps;
-    Ws[VX * PL + q] = to_face<T>(vx);
-    Ws[VY * PL + q] = to_face<T>(vy);
-    Ws[VZ * PL + q] = to_face<T>(vz);
-    Ws[PR * PL + q] = to_face<T>(pr);
-    Ws[RO * PL + q] = to_face<T>(ro);
-    Ws[BX * PL + q] = to_face<T>(bx);
-    Ws[BY * PL + q] = to_face<T>(by);
-    Ws[BZ * PL + q] = to_face<T>(bz);
-    Ws[PS * PL + q] = to_face<T>(ps);
+    T w[NV], pr, ro;
+    u2v_cell<T, OMHD_FAST>(u, f1g, f1g32, ps, w, pr, ro);  // 3D_basic/u2v.f90
+#pragma unroll
+    for (int v = 0; v < NV; ++v) Ws[v * PL + q] = w[v];
     if (own_plane && cx_in && cy_in && gi <= ix - 2 && gj <= jx - 2) {  // u2v.f90:36-45, owner check
-      if (pr <= 0)
-        raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, gk + 1, 0, pr);
-      else if (ro <= 0)
-        raise_error(a.err, OMHD_NEG_DENSITY, gi + 1, gj + 1, gk + 1, 0, ro);
+      if (!(pr > T(0)))
+        raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, gk + 1, 0, to_f64<T>(pr));
+      else if (!(ro > T(0)))
+        raise_error(a.err, OMHD_NEG_DENSITY, gi + 1, gj + 1, gk + 1, 0, to_f64<T>(ro));
     }
   }
 }

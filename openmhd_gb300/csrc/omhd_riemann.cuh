@@ -809,6 +809,71 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
   if constexpr (TAPE == tape::kRecord) *code_io = code_reg;
 }
 
+// u2v.f90:11-27 for one cell, into the face arithmetic's type: w = (vx, vy,
+// vz, p, rho, Bx, By, Bz, psi) with the given (GLM-scaled) psi; pr and ro
+// return p and rho for the positivity check (u2v.f90:36-45).
+// FP64 kernels: the reference's FP64 recovery.  FP32-mixed kernels: binary32
+// recovery where E >= rho v^2 + B^2, i.e. where the internal energy is at
+// least the kinetic plus the magnetic energy, so that the pressure -- a
+// difference of energies -- amplifies the rounding of its inputs at most
+// ~4-fold; FP64 recovery, then rounding, everywhere else (low beta, high
+// Mach, and every unphysical state, whose check then sees FP64 values).
+template <class T, bool FAST>
+__device__ __forceinline__ void u2v_cell(const double (&u)[NV], double f1g, float f1g32, double psi, T (&w)[NV],
+                                         T& pr, T& ro) {
+  if constexpr (sizeof(T) == 4) {
+    const float r = narrow_f64(u[RO]), mx = narrow_f64(u[MX]), my = narrow_f64(u[MY]), mz = narrow_f64(u[MZ]);
+    const float bx = narrow_f64(u[BX]), by = narrow_f64(u[BY]), bz = narrow_f64(u[BZ]), en = narrow_f64(u[EN]);
+    const float ir = __frcp_rn(r);
+    const float vx = mx * ir, vy = my * ir, vz = mz * ir;
+    const float rv2 = vx * mx + vy * my + vz * mz;
+    const float B2 = bx * bx + by * by + bz * bz;
+    if (en >= rv2 + B2) {
+      w[VX] = vx;
+      w[VY] = vy;
+      w[VZ] = vz;
+      w[PR] = f1g32 * (en - 0.5f * (rv2 + B2));
+      w[RO] = r;
+      w[BX] = bx;
+      w[BY] = by;
+      w[BZ] = bz;
+      w[PS] = narrow_f64(psi);
+      pr = w[PR];
+      ro = r;
+      return;
+    }
+  }
+  const double r = u[RO];
+  const double mx = u[MX], my = u[MY], mz = u[MZ];
+  const double ir = rcp_<double, FAST>(r);  // one reciprocal for the three velocities
+  const double vx = divr_<double, FAST>(mx, r, ir), vy = divr_<double, FAST>(my, r, ir),
+               vz = divr_<double, FAST>(mz, r, ir);  // u2v.f90:24
+  const double rv2 = vx * mx + vy * my + vz * mz;
+  const double bx = u[BX], by = u[BY], bz = u[BZ];
+  const double B2 = bx * bx + by * by + bz * bz;
+  const double p = f1g * (u[EN] - 0.5 * (rv2 + B2));  // u2v.f90:27
+  w[VX] = to_face<T>(vx);
+  w[VY] = to_face<T>(vy);
+  w[VZ] = to_face<T>(vz);
+  w[PR] = to_face<T>(p);
+  w[RO] = to_face<T>(r);
+  w[BX] = to_face<T>(bx);
+  w[BY] = to_face<T>(by);
+  w[BZ] = to_face<T>(bz);
+  w[PS] = to_face<T>(psi);
+  pr = sizeof(T) == 8 ? T(p) : w[PR];
+  ro = sizeof(T) == 8 ? T(r) : w[RO];
+}
+
+// x > 0, false for NaN (the IEEE compare; FP64 on the integer pipe in FAST builds)
+template <class T, bool FAST>
+__device__ __forceinline__ bool pos_(T x) {
+  if constexpr (sizeof(T) == 8)
+    return gt0_<FAST>(x);
+  else
+    return x > T(0);
+}
+
 // Fast magnetosonic speed used by set_dt (2D_basic/set_dt.f90:27-34).
 template <class T, bool FAST = false>
 __device__ __forceinline__ T fast_speed(T f1, T B2, T bd, T ro) {

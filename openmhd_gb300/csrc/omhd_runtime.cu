@@ -201,6 +201,8 @@ static std::atomic<int> g_tma_on{1};
 bool tma_staging_enabled() { return g_tma_on.load(std::memory_order_relaxed) != 0; }
 static std::atomic<int> g_pipe3d_on{1};
 bool pipe3d_enabled() { return g_pipe3d_on.load(std::memory_order_relaxed) != 0; }
+static std::atomic<int> g_pipe2d_on{1};
+bool pipe2d_enabled() { return g_pipe2d_on.load(std::memory_order_relaxed) != 0; }
 
 int tma_encode_state_map(CUtensorMap* map, const double* U, int ix, int jx, int nv, int box_x, int box_y) {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
@@ -237,6 +239,7 @@ extern "C" {
 
 void omhd_set_tma_staging(int enable) { g_tma_on.store(enable ? 1 : 0, std::memory_order_relaxed); }
 void omhd_set_3d_pipeline(int enable) { g_pipe3d_on.store(enable ? 1 : 0, std::memory_order_relaxed); }
+void omhd_set_2d_pipeline(int enable) { g_pipe2d_on.store(enable ? 1 : 0, std::memory_order_relaxed); }
 
 int omhd_probe_fastmath(const double* x, long long n, double* out) {
   if (!x || !out || n < 0) return OMHD_BAD_ARG;

@@ -87,5 +87,6 @@ bool tma_staging_enabled();
 // Library-wide switch of the warp-specialised FP64 3D stage kernel (on by
 // default; off: the one-role kernel), for comparisons in tests.
 bool pipe3d_enabled();
+bool pipe2d_enabled();
 
 }  // namespace omhd

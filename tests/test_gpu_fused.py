@@ -193,13 +193,19 @@ def test_mixed_precision_error_vs_fp64(cuda_lib):
     assert np.all(err <= 1e-6), err
 
 
-def test_negative_pressure_is_reported_not_trapped(cuda_lib):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("var,value,status", [(3, -5.0, 1), (4, -0.5, 2)])
+def test_negative_pressure_is_reported_not_trapped(cuda_lib, precision, var, value, status):
+    """E < 0 (negative pressure) or rho < 0 (negative density) in one cell is
+    reported with the cell's Fortran index (u2v.f90:34-43), in FP64 and in the
+    FP32-mixed path (whose binary32 recovery hands every such cell to the FP64
+    recovery, or, for rho < 0, reports it from its own binary32 values)."""
     from openmhd_gb300 import Solver, orszag_tang
 
-    cfg, model = orszag_tang(32)
+    cfg, model = orszag_tang(32, precision=precision)
     s = Solver(cfg).init_model(model)
     U = s.get_state_numpy()
-    U[3, 10, 12] = -5.0  # E < 0 at Fortran (13, 11)
+    U[var, 10, 12] = value  # at Fortran (13, 11)
     s.put_state(U)
     s.step(2)
     import ctypes as C
@@ -207,7 +213,7 @@ def test_negative_pressure_is_reported_not_trapped(cuda_lib):
 
     si = _lib.StepInfo()
     st = s.lib.omhd_solver_sync(s._h, C.byref(si))
-    assert st == 1 and si.status == 1
+    assert st == 1 and si.status == status
     e = _lib.ErrorInfo()
     s.lib.omhd_solver_last_error(s._h, C.byref(e))
     assert (e.i, e.j) == (13, 11)
