@@ -61,9 +61,47 @@ __device__ __forceinline__ double eta3(int kind, double x, double y, double z) {
 }
 
 // eta / dx of the Harris resistivity, eta = 1e-3 + exp(-(x^2+z^2)/4)/60, from
-// the factors ex = exp(-x^2/4) and ez = exp(-z^2/4)
-__device__ __forceinline__ double harris_eta_dx(double ex, double ez, double inv_dx) {
-  return (1.0e-3 + (1.0 / 60.0) * (ex * ez)) * inv_dx;
+// the factors ex = exp(-x^2/4) and ez = exp(-z^2/4), in the arithmetic type R
+template <class R>
+__device__ __forceinline__ R harris_eta_dx(R ex, R ez, R inv_dx) {
+  return (R(1.0e-3) + R(1.0 / 60.0) * (ex * ez)) * inv_dx;
+}
+
+// Resistive terms of the FP32-mixed kernels (flux_resistive.cuf:87-135) in
+// binary32, added to the binary32 face flux they belong to.  Each current
+// component is a difference of cell-centred B across the face plus a quarter
+// of a four-point transverse difference; the four-point sums are formed as two
+// neighbour differences, which binary32 subtracts exactly when the neighbours
+// are within a factor of two (Sterbenz), so the current keeps its relative
+// precision where it is small.  b(var, dx, dy, dz) reads B of the cell at that
+// offset from the face's lower cell; the face normal is axis n (1, 2, 3).
+template <int n, class BF>
+__device__ __forceinline__ void resist_face_f32(const BF& b, float eta_dx, float (&Fo)[NV]) {
+  if constexpr (n == 1) {  // x face (:87-101)
+    const float JyS = (b(BZ, 0, 0, 0) - b(BZ, 1, 0, 0)) +
+                      0.25f * ((b(BX, 0, 0, 1) - b(BX, 0, 0, -1)) + (b(BX, 1, 0, 1) - b(BX, 1, 0, -1)));
+    const float JzS = (b(BY, 1, 0, 0) - b(BY, 0, 0, 0)) -
+                      0.25f * ((b(BX, 0, 1, 0) - b(BX, 0, -1, 0)) + (b(BX, 1, 1, 0) - b(BX, 1, -1, 0)));
+    Fo[EN] += 0.5f * eta_dx * (JyS * (b(BZ, 0, 0, 0) + b(BZ, 1, 0, 0)) - JzS * (b(BY, 0, 0, 0) + b(BY, 1, 0, 0)));
+    Fo[BY] -= eta_dx * JzS;
+    Fo[BZ] += eta_dx * JyS;
+  } else if constexpr (n == 2) {  // y face (:104-118)
+    const float JxS = (b(BZ, 0, 1, 0) - b(BZ, 0, 0, 0)) -
+                      0.25f * ((b(BY, 0, 0, 1) - b(BY, 0, 0, -1)) + (b(BY, 0, 1, 1) - b(BY, 0, 1, -1)));
+    const float JzS = (b(BX, 0, 0, 0) - b(BX, 0, 1, 0)) +
+                      0.25f * ((b(BY, 1, 0, 0) - b(BY, -1, 0, 0)) + (b(BY, 1, 1, 0) - b(BY, -1, 1, 0)));
+    Fo[EN] += 0.5f * eta_dx * (JzS * (b(BX, 0, 0, 0) + b(BX, 0, 1, 0)) - JxS * (b(BZ, 0, 0, 0) + b(BZ, 0, 1, 0)));
+    Fo[BX] += eta_dx * JzS;
+    Fo[BZ] -= eta_dx * JxS;
+  } else {  // z face (:121-135)
+    const float JyS = (b(BX, 0, 0, 1) - b(BX, 0, 0, 0)) -
+                      0.25f * ((b(BZ, 1, 0, 0) - b(BZ, -1, 0, 0)) + (b(BZ, 1, 0, 1) - b(BZ, -1, 0, 1)));
+    const float JxS = (b(BY, 0, 0, 0) - b(BY, 0, 0, 1)) +
+                      0.25f * ((b(BZ, 0, 1, 0) - b(BZ, 0, -1, 0)) + (b(BZ, 0, 1, 1) - b(BZ, 0, -1, 1)));
+    Fo[EN] += 0.5f * eta_dx * (JxS * (b(BY, 0, 0, 0) + b(BY, 0, 0, 1)) - JyS * (b(BX, 0, 0, 0) + b(BX, 0, 0, 1)));
+    Fo[BX] -= eta_dx * JyS;
+    Fo[BY] += eta_dx * JxS;
+  }
 }
 
 // Load + convert one z plane (global index gk, any value; mapped by the z bc)
@@ -149,19 +187,20 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
   // exponential is tabulated over this CTA's x columns (cell centres ex_c and
   // x faces ex_f, index q = i - gi0 + 1) and z chunk (ez_c, ez_f at z faces,
   // index p = k - k0 + 1), one exp per entry instead of one per face.
-  __shared__ double ex_c[TX + 2], ex_f[TX + 2], ez_c[ZCHUNK + 2], ez_f[ZCHUNK + 2];
+  __shared__ T ex_c[TX + 2], ex_f[TX + 2], ez_c[ZCHUNK + 2], ez_f[ZCHUNK + 2];
   const bool sep_eta = OMHD_FAST && a.eta_kind == OMHD_ETA_HARRIS_XZ;
   const double inv_dx = 1.0 / a.dx;
+  const T inv_dx_t = T(inv_dx);
   if (sep_eta) {
     for (int q = tid; q < 2 * (TX + 2) + 2 * (ZCHUNK + 2); q += NT) {
       if (q < 2 * (TX + 2)) {
         const int p = q % (TX + 2);
         const double x = a.xc[min(gi0 - 1 + p, ix - 1)] + (q >= TX + 2 ? 0.5 * a.dx : 0.0);
-        (q < TX + 2 ? ex_c : ex_f)[p] = exp(-(x * x) / 4.0);
+        (q < TX + 2 ? ex_c : ex_f)[p] = to_face<T>(exp(-(x * x) / 4.0));
       } else {
         const int r = q - 2 * (TX + 2), p = r % (ZCHUNK + 2);
         const double z = a.zc[min(k0 - 1 + p, kx - 1)] + (r >= ZCHUNK + 2 ? 0.5 * a.dx : 0.0);
-        (r < ZCHUNK + 2 ? ez_c : ez_f)[p] = exp(-(z * z) / 4.0);
+        (r < ZCHUNK + 2 ? ez_c : ez_f)[p] = to_face<T>(exp(-(z * z) / 4.0));
       }
     }
   }
@@ -192,19 +231,24 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
     for (int v = 0; v < NV; ++v) Fzp[v] = to_f64<T>(Fo[v]);
     if (resist && own) {  // z face k0-1/2 (flux_resistive.cuf:121-135)
       const int k = k0 - 1;
-      auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, oc + dxo + dyo * RX)); };
-      const double eta_dx = sep_eta ? harris_eta_dx(ex_c[tx + 1], ez_f[0], inv_dx)
-                                    : eta3(a.eta_kind, a.xc[gi], a.yc[gj], a.zc[k] + 0.5 * a.dx) / a.dx;
-      const double JyS = (B(BX, 0, 0, 1) - B(BX, 0, 0, 0)) -
-                         0.25 * (B(BZ, 1, 0, 0) + B(BZ, 1, 0, 1) - B(BZ, -1, 0, 0) - B(BZ, -1, 0, 1));
-      const double JxS = -(B(BY, 0, 0, 1) - B(BY, 0, 0, 0)) +
-                         0.25 * (B(BZ, 0, 1, 0) + B(BZ, 0, 1, 1) - B(BZ, 0, -1, 0) - B(BZ, 0, -1, 1));
-      Fzp[EN] = Fzp[EN] + 0.5 * eta_dx * (JxS * (B(BY, 0, 0, 0) + B(BY, 0, 0, 1)) - JyS * (B(BX, 0, 0, 0) + B(BX, 0, 0, 1)));
-      Fzp[BX] = Fzp[BX] - eta_dx * JyS;
-      Fzp[BY] = Fzp[BY] + eta_dx * JxS;
-      if (sizeof(T) == 4) {  // keep the face value the mixed build would round to
+      if constexpr (sizeof(T) == 4) {
+        auto b = [&](int var, int dxo, int dyo, int dzo) { return Wv(k + dzo, var, oc + dxo + dyo * RX); };
+        const float eta_dx = sep_eta ? harris_eta_dx<T>(ex_c[tx + 1], ez_f[0], inv_dx_t)
+                                     : narrow_f64(eta3(a.eta_kind, a.xc[gi], a.yc[gj], a.zc[k] + 0.5 * a.dx) / a.dx);
+        resist_face_f32<3>(b, eta_dx, Fo);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) Fzp[v] = to_f64<T>(to_face<T>(Fzp[v]));
+        for (int v = 0; v < NV; ++v) Fzp[v] = to_f64<T>(Fo[v]);
+      } else {
+        auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, oc + dxo + dyo * RX)); };
+        const double eta_dx = sep_eta ? harris_eta_dx<double>(ex_c[tx + 1], ez_f[0], inv_dx)
+                                      : eta3(a.eta_kind, a.xc[gi], a.yc[gj], a.zc[k] + 0.5 * a.dx) / a.dx;
+        const double JyS = (B(BX, 0, 0, 1) - B(BX, 0, 0, 0)) -
+                           0.25 * (B(BZ, 1, 0, 0) + B(BZ, 1, 0, 1) - B(BZ, -1, 0, 0) - B(BZ, -1, 0, 1));
+        const double JxS = -(B(BY, 0, 0, 1) - B(BY, 0, 0, 0)) +
+                           0.25 * (B(BZ, 0, 1, 0) + B(BZ, 0, 1, 1) - B(BZ, 0, -1, 0) - B(BZ, 0, -1, 1));
+        Fzp[EN] = Fzp[EN] + 0.5 * eta_dx * (JxS * (B(BY, 0, 0, 0) + B(BY, 0, 0, 1)) - JyS * (B(BX, 0, 0, 0) + B(BX, 0, 0, 1)));
+        Fzp[BX] = Fzp[BX] - eta_dx * JyS;
+        Fzp[BY] = Fzp[BY] + eta_dx * JxS;
       }
     }
   }
@@ -269,16 +313,23 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
         const int g = gi0 - 1 + fx, gjj = gj0 + cy;
         if (g >= 0 && g <= ix - 2 && gjj <= jx - 2) {
           const int o = (cy + 2) * RX + (fx + 1);
-          auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, o + dxo + dyo * RX)); };
-          const double eta_dx = sep_eta ? harris_eta_dx(ex_f[fx], ez_c[k - k0 + 1], inv_dx)
-                                        : eta3(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gjj], a.zc[k]) / a.dx;
-          const double JyS = -(B(BZ, 1, 0, 0) - B(BZ, 0, 0, 0)) +
-                             0.25 * (B(BX, 0, 0, 1) + B(BX, 1, 0, 1) - B(BX, 0, 0, -1) - B(BX, 1, 0, -1));
-          const double JzS = (B(BY, 1, 0, 0) - B(BY, 0, 0, 0)) -
-                             0.25 * (B(BX, 0, 1, 0) + B(BX, 1, 1, 0) - B(BX, 0, -1, 0) - B(BX, 1, -1, 0));
-          Fo[EN] = to_face<T>(to_f64<T>(Fo[EN]) + 0.5 * eta_dx * (JyS * (B(BZ, 0, 0, 0) + B(BZ, 1, 0, 0)) - JzS * (B(BY, 0, 0, 0) + B(BY, 1, 0, 0))));
-          Fo[BY] = to_face<T>(to_f64<T>(Fo[BY]) - eta_dx * JzS);
-          Fo[BZ] = to_face<T>(to_f64<T>(Fo[BZ]) + eta_dx * JyS);
+          if constexpr (sizeof(T) == 4) {
+            auto b = [&](int var, int dxo, int dyo, int dzo) { return Wv(k + dzo, var, o + dxo + dyo * RX); };
+            const float eta_dx = sep_eta ? harris_eta_dx<T>(ex_f[fx], ez_c[k - k0 + 1], inv_dx_t)
+                                         : narrow_f64(eta3(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gjj], a.zc[k]) / a.dx);
+            resist_face_f32<1>(b, eta_dx, Fo);
+          } else {
+            auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, o + dxo + dyo * RX)); };
+            const double eta_dx = sep_eta ? harris_eta_dx<double>(ex_f[fx], ez_c[k - k0 + 1], inv_dx)
+                                          : eta3(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gjj], a.zc[k]) / a.dx;
+            const double JyS = -(B(BZ, 1, 0, 0) - B(BZ, 0, 0, 0)) +
+                               0.25 * (B(BX, 0, 0, 1) + B(BX, 1, 0, 1) - B(BX, 0, 0, -1) - B(BX, 1, 0, -1));
+            const double JzS = (B(BY, 1, 0, 0) - B(BY, 0, 0, 0)) -
+                               0.25 * (B(BX, 0, 1, 0) + B(BX, 1, 1, 0) - B(BX, 0, -1, 0) - B(BX, 1, -1, 0));
+            Fo[EN] = Fo[EN] + 0.5 * eta_dx * (JyS * (B(BZ, 0, 0, 0) + B(BZ, 1, 0, 0)) - JzS * (B(BY, 0, 0, 0) + B(BY, 1, 0, 0)));
+            Fo[BY] = Fo[BY] - eta_dx * JzS;
+            Fo[BZ] = Fo[BZ] + eta_dx * JyS;
+          }
         }
       }
 #pragma unroll
@@ -335,16 +386,23 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
         const int gii = gi0 + cx, g = gj0 - 1 + fy;
         if (g >= 0 && g <= jx - 2 && gii <= ix - 2) {
           const int o = (fy + 1) * RX + (cx + 2);
-          auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, o + dxo + dyo * RX)); };
-          const double eta_dx = sep_eta ? harris_eta_dx(ex_c[cx + 1], ez_c[k - k0 + 1], inv_dx)
-                                        : eta3(a.eta_kind, a.xc[gii], a.yc[g] + 0.5 * a.dx, a.zc[k]) / a.dx;
-          const double JxS = (B(BZ, 0, 1, 0) - B(BZ, 0, 0, 0)) -
-                             0.25 * (B(BY, 0, 0, 1) + B(BY, 0, 1, 1) - B(BY, 0, 0, -1) - B(BY, 0, 1, -1));
-          const double JzS = -(B(BX, 0, 1, 0) - B(BX, 0, 0, 0)) +
-                             0.25 * (B(BY, 1, 0, 0) + B(BY, 1, 1, 0) - B(BY, -1, 0, 0) - B(BY, -1, 1, 0));
-          Fo[EN] = to_face<T>(to_f64<T>(Fo[EN]) + 0.5 * eta_dx * (JzS * (B(BX, 0, 0, 0) + B(BX, 0, 1, 0)) - JxS * (B(BZ, 0, 0, 0) + B(BZ, 0, 1, 0))));
-          Fo[BX] = to_face<T>(to_f64<T>(Fo[BX]) + eta_dx * JzS);
-          Fo[BZ] = to_face<T>(to_f64<T>(Fo[BZ]) - eta_dx * JxS);
+          if constexpr (sizeof(T) == 4) {
+            auto b = [&](int var, int dxo, int dyo, int dzo) { return Wv(k + dzo, var, o + dxo + dyo * RX); };
+            const float eta_dx = sep_eta ? harris_eta_dx<T>(ex_c[cx + 1], ez_c[k - k0 + 1], inv_dx_t)
+                                         : narrow_f64(eta3(a.eta_kind, a.xc[gii], a.yc[g] + 0.5 * a.dx, a.zc[k]) / a.dx);
+            resist_face_f32<2>(b, eta_dx, Fo);
+          } else {
+            auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, o + dxo + dyo * RX)); };
+            const double eta_dx = sep_eta ? harris_eta_dx<double>(ex_c[cx + 1], ez_c[k - k0 + 1], inv_dx)
+                                          : eta3(a.eta_kind, a.xc[gii], a.yc[g] + 0.5 * a.dx, a.zc[k]) / a.dx;
+            const double JxS = (B(BZ, 0, 1, 0) - B(BZ, 0, 0, 0)) -
+                               0.25 * (B(BY, 0, 0, 1) + B(BY, 0, 1, 1) - B(BY, 0, 0, -1) - B(BY, 0, 1, -1));
+            const double JzS = -(B(BX, 0, 1, 0) - B(BX, 0, 0, 0)) +
+                               0.25 * (B(BY, 1, 0, 0) + B(BY, 1, 1, 0) - B(BY, -1, 0, 0) - B(BY, -1, 1, 0));
+            Fo[EN] = Fo[EN] + 0.5 * eta_dx * (JzS * (B(BX, 0, 0, 0) + B(BX, 0, 1, 0)) - JxS * (B(BZ, 0, 0, 0) + B(BZ, 0, 1, 0)));
+            Fo[BX] = Fo[BX] + eta_dx * JzS;
+            Fo[BZ] = Fo[BZ] - eta_dx * JxS;
+          }
         }
       }
 #pragma unroll
@@ -379,19 +437,24 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
 #pragma unroll
       for (int v = 0; v < NV; ++v) Fzc[v] = to_f64<T>(Fo[v]);
       if (resist && own) {  // flux_resistive.cuf:121-135
-        auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, oc + dxo + dyo * RX)); };
-        const double eta_dx = sep_eta ? harris_eta_dx(ex_c[tx + 1], ez_f[k - k0 + 1], inv_dx)
-                                      : eta3(a.eta_kind, a.xc[gi], a.yc[gj], a.zc[k] + 0.5 * a.dx) / a.dx;
-        const double JyS = (B(BX, 0, 0, 1) - B(BX, 0, 0, 0)) -
-                           0.25 * (B(BZ, 1, 0, 0) + B(BZ, 1, 0, 1) - B(BZ, -1, 0, 0) - B(BZ, -1, 0, 1));
-        const double JxS = -(B(BY, 0, 0, 1) - B(BY, 0, 0, 0)) +
-                           0.25 * (B(BZ, 0, 1, 0) + B(BZ, 0, 1, 1) - B(BZ, 0, -1, 0) - B(BZ, 0, -1, 1));
-        Fzc[EN] = Fzc[EN] + 0.5 * eta_dx * (JxS * (B(BY, 0, 0, 0) + B(BY, 0, 0, 1)) - JyS * (B(BX, 0, 0, 0) + B(BX, 0, 0, 1)));
-        Fzc[BX] = Fzc[BX] - eta_dx * JyS;
-        Fzc[BY] = Fzc[BY] + eta_dx * JxS;
-        if (sizeof(T) == 4) {
+        if constexpr (sizeof(T) == 4) {
+          auto b = [&](int var, int dxo, int dyo, int dzo) { return Wv(k + dzo, var, oc + dxo + dyo * RX); };
+          const float eta_dx = sep_eta ? harris_eta_dx<T>(ex_c[tx + 1], ez_f[k - k0 + 1], inv_dx_t)
+                                       : narrow_f64(eta3(a.eta_kind, a.xc[gi], a.yc[gj], a.zc[k] + 0.5 * a.dx) / a.dx);
+          resist_face_f32<3>(b, eta_dx, Fo);
 #pragma unroll
-          for (int v = 0; v < NV; ++v) Fzc[v] = to_f64<T>(to_face<T>(Fzc[v]));
+          for (int v = 0; v < NV; ++v) Fzc[v] = to_f64<T>(Fo[v]);
+        } else {
+          auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, oc + dxo + dyo * RX)); };
+          const double eta_dx = sep_eta ? harris_eta_dx<double>(ex_c[tx + 1], ez_f[k - k0 + 1], inv_dx)
+                                        : eta3(a.eta_kind, a.xc[gi], a.yc[gj], a.zc[k] + 0.5 * a.dx) / a.dx;
+          const double JyS = (B(BX, 0, 0, 1) - B(BX, 0, 0, 0)) -
+                             0.25 * (B(BZ, 1, 0, 0) + B(BZ, 1, 0, 1) - B(BZ, -1, 0, 0) - B(BZ, -1, 0, 1));
+          const double JxS = -(B(BY, 0, 0, 1) - B(BY, 0, 0, 0)) +
+                             0.25 * (B(BZ, 0, 1, 0) + B(BZ, 0, 1, 1) - B(BZ, 0, -1, 0) - B(BZ, 0, -1, 1));
+          Fzc[EN] = Fzc[EN] + 0.5 * eta_dx * (JxS * (B(BY, 0, 0, 0) + B(BY, 0, 0, 1)) - JyS * (B(BX, 0, 0, 0) + B(BX, 0, 0, 1)));
+          Fzc[BX] = Fzc[BX] - eta_dx * JyS;
+          Fzc[BY] = Fzc[BY] + eta_dx * JxS;
         }
       }
     }
