@@ -213,7 +213,7 @@ def test_negative_pressure_is_reported_not_trapped(cuda_lib, precision, var, val
 
     si = _lib.StepInfo()
     st = s.lib.omhd_solver_sync(s._h, C.byref(si))
-    assert st == 1 and si.status == status
+    assert st == status and si.status == status
     e = _lib.ErrorInfo()
     s.lib.omhd_solver_last_error(s._h, C.byref(e))
     assert (e.i, e.j) == (13, 11)
