@@ -51,24 +51,43 @@ def _load_flops(name: str = "flops_kh2d.txt"):
 
 
 def _load_flops_split(name: str):
-    """(total, face-flux part, rest) flops per cell-update from a profiles/ flop
-    count: the face part (limiters, face fixes, Riemann solver, resistive face
-    terms) is what the FP32-mixed kernels compute in FP32, the rest (u2v, CFL,
-    GLM, RK update) their FP64 residual."""
+    """(total, face-flux part, rest, u2v part of the rest) flops per cell-update
+    from a profiles/ flop count: the face part (limiters, face fixes, Riemann
+    solver, resistive face terms) is what the FP32-mixed kernels compute in
+    FP32, the rest (u2v, CFL, GLM, RK update) their FP64 residual, except the
+    u2v part, which they run in FP32 in cells whose internal energy is at least
+    the kinetic plus magnetic energy."""
     p = os.path.join(ROOT, "profiles", name)
     txt = open(p).read()
     get = lambda k: float(re.search(k + r":\s*([0-9.]+)", txt).group(1))  # noqa: E731
-    return get("flops_per_cell_update"), get("face_flux_flops_per_cell_update"), get("rest_flops_per_cell_update")
+    return (get("flops_per_cell_update"), get("face_flux_flops_per_cell_update"), get("rest_flops_per_cell_update"),
+            get("u2v_flops_per_cell_update"))
+
+
+def _u2v_fp64_share(states) -> float:
+    """Share of the cells whose primitives the FP32-mixed kernels recover in
+    FP64 (E < rho v^2 + B^2: the internal energy below the kinetic plus
+    magnetic energy), over conserved states (9, ...) on the device."""
+    n = low = 0
+    for U in states:
+        U = U.reshape(9, -1)
+        rv2 = (U[0] * U[0] + U[1] * U[1] + U[2] * U[2]) / U[4]
+        B2 = U[5] * U[5] + U[6] * U[6] + U[7] * U[7]
+        low += int((U[3] < rv2 + B2).sum())
+        n += U.shape[1]
+    return low / max(n, 1)
 
 
 def _mixed_roofline(cells_per_s: float, split, fp64_peak_gflops: float, fp32_peak_gflops: float,
-                    hbm_peak_gbs: float, bytes_per_cu: float = BYTES_PER_CELL_UPDATE_2D):
+                    hbm_peak_gbs: float, bytes_per_cu: float = BYTES_PER_CELL_UPDATE_2D, u2v_fp64_share: float = 1.0):
     """Roofline of an FP32-mixed run: the time per cell-update is bounded by
-    the slowest of its FP64 residual flops at the FP64 peak, its FP32 face-flux
-    flops at the FP32 peak and its bytes at the HBM peak.  `achieved`/`frac`
+    the slowest of its FP64 residual flops at the FP64 peak, its FP32 flops
+    (face work, and the u2v of the cells recovered in FP32: 1 - u2v_fp64_share
+    of them) at the FP32 peak and its bytes at the HBM peak.  `achieved`/`frac`
     are those of the binding resource (the FP64 residual on GB300, whose FP64
     pipe is 1/64 of its FP32 rate); `roof_frac` = roof time / measured time."""
-    _, face, rest = split
+    _, face, rest, u2v = split
+    rest, face = rest - u2v * (1.0 - u2v_fp64_share), face + u2v * (1.0 - u2v_fp64_share)
     t64 = rest / (fp64_peak_gflops * 1e9)
     t32 = face / (fp32_peak_gflops * 1e9)
     tb = bytes_per_cu / (hbm_peak_gbs * 1e9)
@@ -83,6 +102,7 @@ def _mixed_roofline(cells_per_s: float, split, fp64_peak_gflops: float, fp32_pea
     out["achieved"], out["peak"], out["unit"], out["frac"] = (out[bound]["achieved"], out[bound]["peak"],
                                                               out[bound]["unit"], out[bound]["frac"])
     out["roof_frac"] = max(t64, t32, tb) * cells_per_s
+    out["u2v_fp64_share"] = u2v_fp64_share
     return out
 
 
@@ -402,6 +422,7 @@ def run_ours(args):
     t_mx = e0.elapsed_time(e1) / 1e3
     Um = m.get_state_numpy()
     mixed_err = _errors(Um[:, 1:-1, 1:-1], U64[:, 1:-1, 1:-1])
+    mixed_share = _u2v_fp64_share([m.U[:, 1:-1, 1:-1]])
     del m
 
     # ---- end to end through the C ABI with host buffers ----
@@ -472,7 +493,8 @@ def run_ours(args):
         "clocks": clk.summary(),
         "mixed": {"value": ws * cells * args.steps / t_mx, "speedup_vs_fp64": t_fp64 / t_mx,
                   "roofline": _mixed_roofline(cells * args.steps / t_mx, _load_flops_split("flops_kh2d.txt"),
-                                              fp64_peak, fp32_peak, peaks.get("hbm_gbs", 6800.0)),
+                                              fp64_peak, fp32_peak, peaks.get("hbm_gbs", 6800.0),
+                                              u2v_fp64_share=mixed_share),
                   "error_vs_fp64": mixed_err, "status": im.status,
                   "steps_compared": args.warmup + args.steps},
         "peaks_in_run": {"fp64_gflops": fp64_peak, "fp32_gflops": fp32_peak,
@@ -560,16 +582,22 @@ def run_batched(args, fp64_peak: float = float("nan"), fp32_peak: float = float(
     ref.step(total_steps - 3 - args.steps)
     ref.sync()
     errs, owns, lis = [], [], []
+    low = cnt = 0.0
     for i in range(len(cfgs)):
-        e = _errors(ens.member_state(i)[:, 1:-1, 1:-1], ref.member_state(i)[:, 1:-1, 1:-1])
+        Ui = ens.member_state(i)[:, 1:-1, 1:-1]
+        low += _u2v_fp64_share([Ui]) * Ui[0].size
+        cnt += Ui[0].size
+        e = _errors(Ui, ref.member_state(i)[:, 1:-1, 1:-1])
         errs.append(e["max_scaled_l1"])
         owns.append(e["max_own_norm_rel_l1_significant"])
         lis.append(max(e["linf"].values()))
     del ref
+    batch_share = low / max(cnt, 1.0)
     peaks, _ = _peaks()
     split = _load_flops_split("flops_ensemble2d.txt")
     return {"value": updates / t, "unit": "cell-updates/s", "members": len(cfgs),
-            "roofline": _mixed_roofline(updates / t, split, fp64_peak, fp32_peak, peaks.get("hbm_gbs", 6800.0)),
+            "roofline": _mixed_roofline(updates / t, split, fp64_peak, fp32_peak, peaks.get("hbm_gbs", 6800.0),
+                                        u2v_fp64_share=batch_share),
             "fp64_roofline": _fp64_roofline(updates64 / t64, split[0], fp64_peak, peaks.get("hbm_gbs", 6800.0)),
             "max_member_own_norm_rel_l1_vs_fp64": max(owns),
             "median_member_own_norm_rel_l1_vs_fp64": float(np.median(owns)),
@@ -679,7 +707,8 @@ def run_3d(args, fp64_peak: float = float("nan"), fp32_peak: float = float("nan"
             out[prec]["roofline"] = _fp64_roofline(cells * steps / t, split[0], fp64_peak, peaks.get("hbm_gbs", 6800.0))
         else:
             out[prec]["roofline"] = _mixed_roofline(cells * steps / t, split, fp64_peak, fp32_peak,
-                                                    peaks.get("hbm_gbs", 6800.0))
+                                                    peaks.get("hbm_gbs", 6800.0),
+                                                    u2v_fp64_share=_u2v_fp64_share([s.U[:, 1:-1, 1:-1, 1:-1]]))
         states[prec] = s
     out["mixed"]["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     out["mixed"]["error_vs_fp64"] = _errors(states["mixed"].U[:, 1:-1, 1:-1, 1:-1], states["fp64"].U[:, 1:-1, 1:-1, 1:-1])
@@ -882,9 +911,10 @@ def run_accuracy(args):
 def _ensemble_worst_members(curve, control: bool, nworst: int = 3):
     """The batched configuration's members with the largest FP32-mixed error
     against FP64 after its 500 steps (both ensembles in one batched launch per
-    stage, as the bench's batched leg runs them), then each of those members
-    alone: its error curve, and with control=True the same member in FP64
-    against FP64 without multiply-add contraction (round-off growth)."""
+    stage with the autotuned tiling, as the bench's batched leg runs them),
+    then each of those members alone: its error curve, and with control=True
+    the same member in FP64 against FP64 without multiply-add contraction
+    (round-off growth)."""
     import numpy as np
     import torch
 
@@ -894,6 +924,8 @@ def _ensemble_worst_members(curve, control: bool, nworst: int = 3):
     cfg64, _ = batched_problem_set(128, seed=0, precision="fp64")
     mx = Ensemble(cfgs).init_models(models)
     r64 = Ensemble(cfg64).init_models(models)
+    kind, cps, _ = mx.autotune(steps=2)  # the tiling the batched leg runs (the tuner restores the state)
+    r64.set_tiling(kind, cps)
     mx.step(BATCH_STEPS)
     r64.step(BATCH_STEPS)
     mx.sync()

@@ -7,7 +7,9 @@
 // The face reconstruction and flux work of a step (limiters, face fixes,
 // Riemann solver, resistive face terms: the part the FP32-mixed kernels run in
 // FP32) is tallied apart from the rest (u2v, CFL, GLM, RK update, bc: the FP64
-// residual of the mixed kernels).
+// residual of the mixed kernels), and within the rest the conserved-to-
+// primitive recoveries (u2v), which the mixed kernels run in FP32 where the
+// internal energy is at least the kinetic plus magnetic energy.
 // Usage: flopcount <nx> <ny> <steps> [kh|ot]
 //        flopcount <nx> <ny> <nz> <steps> harris   (3D resistive Harris sheet)
 // (prints flops per cell-update, total and split)
@@ -19,8 +21,8 @@
 #include <cstring>
 #include <vector>
 
-static unsigned long long g_count[2] = {0, 0};
-static int g_region = 0;  // 1 inside the face-flux part of a step
+static unsigned long long g_count[3] = {0, 0, 0};
+static int g_region = 0;  // 1 inside the face-flux part of a step, 2 inside u2v
 #define g_flops g_count[g_region]
 
 struct cd {
@@ -54,6 +56,7 @@ inline cd fabs(cd a) { return cd(std::fabs(a.v)); }
 inline cd copysign(cd a, cd b) { return cd(std::copysign(a.v, b.v)); }
 
 #define OMO_FLUX_REGION(on) (g_region = (on))
+#define OMO_U2V_REGION(on) (g_region = (on) ? 2 : 0)
 #define double cd
 #include "omhd_oracle.c"
 #undef double
@@ -61,12 +64,13 @@ inline cd copysign(cd a, cd b) { return cd(std::copysign(a.v, b.v)); }
 
 static void report(const char* what, int nx, int ny, int nz, int steps) {
   const double cells = (double)nx * ny * nz * steps;
-  const unsigned long long tot = g_count[0] + g_count[1];
+  const unsigned long long tot = g_count[0] + g_count[1] + g_count[2];
   printf("workload: %s %dx%dx%d, %d steps\n", what, nx, ny, nz, steps);
   printf("total_flops: %llu\n", tot);
   printf("flops_per_cell_update: %.1f\n", (double)tot / cells);
   printf("face_flux_flops_per_cell_update: %.1f\n", (double)g_count[1] / cells);
-  printf("rest_flops_per_cell_update: %.1f\n", (double)g_count[0] / cells);
+  printf("rest_flops_per_cell_update: %.1f\n", (double)(g_count[0] + g_count[2]) / cells);
+  printf("u2v_flops_per_cell_update: %.1f\n", (double)g_count[2] / cells);
 }
 
 static int harris(int nx, int ny, int nz, int steps) {
@@ -104,7 +108,7 @@ static int harris(int nx, int ny, int nz, int steps) {
   omo_bc(U.data(), c.ix, c.jx, c.kx, 3, &c.bc);
   cd t(0.0), dt(0.0), ch(0.0);
   omo_err e;
-  g_count[0] = g_count[1] = 0;
+  g_count[0] = g_count[1] = g_count[2] = 0;
   g_region = 0;
   for (int s = 0; s < steps; ++s) {
     if (omo_step(&c, U.data(), ws.data(), x.data(), y.data(), z.data(), &t, &dt, &ch, &e)) {
@@ -169,7 +173,7 @@ int main(int argc, char** argv) {
   omo_bc(U.data(), c.ix, c.jx, 1, 2, &c.bc);
   cd t(0.0), dt(0.0), ch(0.0);
   omo_err e;
-  g_count[0] = g_count[1] = 0;
+  g_count[0] = g_count[1] = g_count[2] = 0;
   g_region = 0;
   for (int s = 0; s < steps; ++s) {
     if (omo_step(&c, U.data(), ws.data(), x.data(), y.data(), z.data(), &t, &dt, &ch, &e)) {

@@ -802,10 +802,14 @@ static void limit_all(const omo_cfg* c, const double* U, const double* V, double
     omo_limiter(U + us[q] * n, VL + us[q] * n, VR + us[q] * n, c->ix, c->jx, c->kx, dir, c->lm_type);
 }
 
-/* The flop-counting build (oracle/flopcount.cpp) defines this to tally the
- * face reconstruction and flux work of a step apart from the rest. */
+/* The flop-counting build (oracle/flopcount.cpp) defines these to tally the
+ * face reconstruction and flux work of a step, and its conserved-to-primitive
+ * recoveries, apart from the rest. */
 #ifndef OMO_FLUX_REGION
 #define OMO_FLUX_REGION(on)
+#endif
+#ifndef OMO_U2V_REGION
+#define OMO_U2V_REGION(on)
 #endif
 
 static int half_fluxes(const omo_cfg* c, const double* Ucur, double* V, double* VL, double* VR,
@@ -838,7 +842,9 @@ int omo_step(const omo_cfg* c, double* U, double* ws, const double* x, const dou
   omo_set_gamma(c->gamma);
   if (err) err->code = OMO_OK;
 
+  OMO_U2V_REGION(1);
   st = omo_u2v(U, V, c->ix, c->jx, c->kx, err);
+  OMO_U2V_REGION(0);
   if (st) return st;
   st = omo_set_dt(U, V, &ch, &dt, c->dx, c->dy, c->dz, c->cfl, c->ix, c->jx, c->kx, c->nd, err);
   if (c->eta_kind != OMO_ETA_NONE) omo_set_dt_resistive(&dt, c->dx, c->cfl, c->eta_kind);
@@ -851,7 +857,9 @@ int omo_step(const omo_cfg* c, double* U, double* ws, const double* x, const dou
   else
     omo_rk_std21(U, U1, F, G, H, dt, c->dx, c->dy, c->dz, c->ix, c->jx, c->kx, c->nd);
   omo_bc(U1, c->ix, c->jx, c->kx, c->nd, &c->bc);
+  OMO_U2V_REGION(1);
   st = omo_u2v(U1, V, c->ix, c->jx, c->kx, err);
+  OMO_U2V_REGION(0);
   if (st) return st;
 
   half_fluxes(c, U1, V, VL, VR, Fd, ch, x, y, z);
