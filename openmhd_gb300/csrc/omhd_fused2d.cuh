@@ -60,14 +60,21 @@ struct Geo2 {
 };
 // tile of the single-grid stage kernel per arithmetic type: the FP64 kernel is
 // FP64-pipe bound and gains from the smaller halo of 16x16 tiles; the
-// FP32-mixed kernel (two CTAs per SM) runs faster on 32x8
+// FP32-mixed kernel (two CTAs per SM) runs faster on 32x8 (a build-time
+// constant, for tuning)
+#ifndef OMHD_MIXED_TILE_X
+#define OMHD_MIXED_TILE_X 32
+#endif
+#ifndef OMHD_MIXED_TILE_Y
+#define OMHD_MIXED_TILE_Y 8
+#endif
 template <class T>
 struct GeoFor {
   using type = Geo2<16, 16>;
 };
 template <>
 struct GeoFor<float> {
-  using type = Geo2<32, 8>;
+  using type = Geo2<OMHD_MIXED_TILE_X, OMHD_MIXED_TILE_Y>;
 };
 
 __device__ __forceinline__ int map_index(int g, int n, bool periodic) {

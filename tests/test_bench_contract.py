@@ -66,3 +66,39 @@ def test_failing_leg_is_reported_under_its_key():
 
     assert bench._leg(boom, None) == {"error": "RuntimeError: leg failed"}
     assert bench._leg(lambda a, b: a + b, 1, 2) == 3
+
+
+def test_mixed_roofline_counts_binary32_u2v_as_fp32_work():
+    """The FP32-mixed roofline: the u2v part of the FP64 residual moves to the
+    FP32 side for the share of cells recovered in binary32, the binding
+    resource is the slowest one, and achieved / frac follow from it."""
+    import bench
+
+    total, face, rest, u2v = bench._load_flops_split("flops_kh2d.txt")
+    assert abs(total - (face + rest)) < 0.2 and 0 < u2v < rest
+    split = (total, face, rest, u2v)
+    cps = 1.0e9
+    all64 = bench._mixed_roofline(cps, split, 1250.0, 78000.0, 6800.0, u2v_fp64_share=1.0)
+    none64 = bench._mixed_roofline(cps, split, 1250.0, 78000.0, 6800.0, u2v_fp64_share=0.0)
+    assert all64["bound"] == none64["bound"] == "fp64"
+    assert all64["fp64"]["per_cell_update"] == rest
+    assert abs(none64["fp64"]["per_cell_update"] - (rest - u2v)) < 1e-9
+    assert abs(none64["fp32"]["per_cell_update"] - (face + u2v)) < 1e-9
+    assert abs(none64["frac"] - (rest - u2v) * cps / 1.25e12) < 1e-12
+    assert none64["u2v_fp64_share"] == 0.0
+
+
+def test_u2v_fp64_share_follows_the_energy_test():
+    """Cells with E < rho v^2 + B^2 (internal energy below kinetic plus
+    magnetic) are the ones the FP32-mixed kernels recover in FP64."""
+    import numpy as np
+
+    import bench
+
+    U = np.zeros((9, 4))
+    U[4] = 1.0                       # rho
+    U[0] = [0.0, 1.0, 0.0, 0.0]      # mx
+    U[5] = [0.0, 0.0, 1.0, 0.1]      # Bx
+    U[3] = [1.0, 1.0, 0.9, 1.0]      # E: cell 1 has E = rho v^2, cell 2 E < B^2
+    assert bench._u2v_fp64_share([U]) == 0.25
+    assert bench._u2v_fp64_share([U[:, :2], U[:, 2:]]) == 0.25
