@@ -58,15 +58,16 @@ struct Geo2 {
   }
   static_assert((NV * (RY * RX + 2 * (NXS + NYS))) % 2 == 0, "flux block must start 8-byte aligned");
 };
-// tile of the single-grid stage kernel per arithmetic type: the FP64 kernel is
-// FP64-pipe bound and gains from the smaller halo of 16x16 tiles; the
-// FP32-mixed kernel (two CTAs per SM) runs faster on 32x8 (a build-time
+// tile of the single-grid stage kernel per arithmetic type: 16x16, whose halo
+// is the smallest of the shapes a 288-thread CTA serves (1.5 loaded cells per
+// cell); the FP32-mixed kernel (two CTAs per SM) measured 16x16 / 32x8 / 64x4 at
+// 1.885e9 / 1.868e9 / 1.824e9 cell-updates/s on KH 4096x2048 (a build-time
 // constant, for tuning)
 #ifndef OMHD_MIXED_TILE_X
-#define OMHD_MIXED_TILE_X 32
+#define OMHD_MIXED_TILE_X 16
 #endif
 #ifndef OMHD_MIXED_TILE_Y
-#define OMHD_MIXED_TILE_Y 8
+#define OMHD_MIXED_TILE_Y 16
 #endif
 template <class T>
 struct GeoFor {
