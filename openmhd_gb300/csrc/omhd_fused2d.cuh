@@ -349,6 +349,18 @@ __device__ __forceinline__ void phase_recon(const StageArgs& a, int bxi, int byi
   }
 }
 
+// whether phase_walls changes a face state of this tile (a tile at a
+// non-periodic edge); uniform over the CTA, so the barrier that follows the
+// wall fixes is taken only by the tiles that have some
+template <class G>
+__device__ __forceinline__ bool tile_on_wall(const StageArgs& a, int bxi, int byi) {
+  const int gi0 = 1 + bxi * G::TX, gj0 = 1 + byi * G::TY;
+  const int clx = (a.ix - 2) - gi0 + 1, cly = (a.jx - 2) - gj0 + 1;
+  const bool wx = a.bc_kind[0] != OMHD_BC_PERIODIC && (gi0 == 1 || (clx >= 1 && clx <= G::TX));
+  const bool wy = a.bc_kind[2] != OMHD_BC_PERIODIC && (gj0 == 1 || (cly >= 1 && cly <= G::TY));
+  return wx || wy;
+}
+
 // wall face fixes after phase B: x walls (2D_reconnection/bc.f90:136-165),
 // y walls (2D_KH/bc.f90:55-83)
 template <class T, class G>
@@ -688,7 +700,7 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
   __syncthreads();
   phase_recon<T, G, TAPE>(a, bxi, byi, m, tid, G::NT);
   __syncthreads();
-  if (a.bc_kind[0] != OMHD_BC_PERIODIC || a.bc_kind[2] != OMHD_BC_PERIODIC) {
+  if (tile_on_wall<G>(a, bxi, byi)) {
     phase_walls<T, G>(a, bxi, byi, m, tid, G::NT);
     __syncthreads();
   }
@@ -797,7 +809,6 @@ __global__ void __launch_bounds__(NPW * 32 + PipeGeo::NT, 1)
   const double glmf = ks.glmf;
   const int ntx = (a.ix - 2 + G::TX - 1) / G::TX;
   const int ntiles = ntx * ((a.jx - 2 + G::TY - 1) / G::TY);
-  const bool walls = a.bc_kind[0] != OMHD_BC_PERIODIC || a.bc_kind[2] != OMHD_BC_PERIODIC;
   double vmax = 0.0;
   if (threadIdx.x < NP) {  // producers: A, B, wall fixes of tiles blockIdx.x, +gridDim.x, ...
     const int t = threadIdx.x;
@@ -846,7 +857,7 @@ __global__ void __launch_bounds__(NPW * 32 + PipeGeo::NT, 1)
       const int wn = w + (int)gridDim.x;
       if (t == 0 && !tma_lost && wn < ntiles && staged(wn)) issue(wn);
       phase_recon<double, G, TAPE>(a, w % ntx, w / ntx, m, t, NP);
-      if (walls) {
+      if (tile_on_wall<G>(a, w % ntx, w / ntx)) {
         named_bar_sync(kPipeBarProd, NP);
         phase_walls<double, G>(a, w % ntx, w / ntx, m, t, NP);
       }
