@@ -87,7 +87,8 @@ enum {
 enum {
   OMHD_PREC_FP64 = 0,        /* FP64 throughout, multiply-add contraction on */
   OMHD_PREC_FP64_PARITY = 1, /* FP64, no contraction: the reference's IEEE op sequence */
-  OMHD_PREC_MIXED = 2        /* FP32 reconstruction + Riemann solver, FP64 state/update/dt */
+  OMHD_PREC_MIXED = 2        /* FP32 reconstruction, Riemann solver and resistive face terms; FP64 state,
+                                update and dt; u2v in FP32 except where E < rho v^2 + B^2 (low beta) */
 };
 
 /* ======================================================================
