@@ -932,34 +932,46 @@ __global__ void __launch_bounds__(G::NT, sizeof(T) == 4 ? 2 : 1) k_batch2d(const
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red32[32];
   __shared__ unsigned int is_last;
-  __shared__ int skip_s, w_s;
-  __shared__ StageScalars<T> ks;
-  for (;;) {
-    if (threadIdx.x == 0) w_s = atomicAdd(queue, 1);
-    __syncthreads();
-    const int w = w_s;  // uniform; rewritten only after the barrier that ends this item
-    if (w >= total_tiles) break;
-    int lo = 0, hi = ngrids - 1;  // last grid with tile_start <= w
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (tile_start[mid] <= w)
-        lo = mid;
-      else
-        hi = mid - 1;
+  // the work item's descriptor, written by thread 0 before the barrier that
+  // opens the item: two slots by item parity, so that thread 0 fills the next
+  // item's slot while the other threads may still be reading this item's
+  // (one barrier per item instead of three: every thread passes the opening
+  // barrier of item i+1 only after finishing item i, so a slot is rewritten
+  // only after every read of it)
+  __shared__ int w_s[2], grid_s[2], skip_s[2];
+  __shared__ StageScalars<T> ks[2];
+  for (int it = 0;; ++it) {
+    const int sl = it & 1;
+    if (threadIdx.x == 0) {
+      const int w = atomicAdd(queue, 1);
+      w_s[sl] = w;
+      if (w < total_tiles) {
+        int lo = 0, hi = ngrids - 1;  // last grid with tile_start <= w
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (tile_start[mid] <= w)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        grid_s[sl] = lo;
+        const StageArgs& g = args[lo];
+        skip_s[sl] = g.st->done || *(volatile int*)&g.err->code;
+        stage_scalars<T>(g, g.st, ks[sl]);
+      }
     }
+    __syncthreads();
+    const int w = w_s[sl];  // uniform over the CTA
+    if (w >= total_tiles) break;
+    const int lo = grid_s[sl];
     const StageArgs& a = args[lo];
     StepState* st = a.st;
     const int local = w - tile_start[lo];
     const int ntx = (a.ix - 2 + G::TX - 1) / G::TX;
     const int ntiles = ntx * ((a.jx - 2 + G::TY - 1) / G::TY);
-    if (threadIdx.x == 0) {
-      skip_s = st->done || *(volatile int*)&a.err->code;
-      stage_scalars<T>(a, st, ks);
-    }
-    __syncthreads();
-    const bool skip = skip_s;  // uniform over the CTA
+    const bool skip = skip_s[sl];
     double vcell = 0.0;
-    if (!skip) vcell = stage2d_tile<T, FLUX, G>(a, local % ntx, local / ntx, smem_raw, ks);
+    if (!skip) vcell = stage2d_tile<T, FLUX, G>(a, local % ntx, local / ntx, smem_raw, ks[sl]);
     if (!skip && a.stage == 2) {
       const double bm = block_max_pos(vcell, red32);
       if (threadIdx.x == 0) {
@@ -974,7 +986,8 @@ __global__ void __launch_bounds__(G::NT, sizeof(T) == 4 ? 2 : 1) k_batch2d(const
         finalize_step(st, sc, a.err, 1);
       }
     }
-    __syncthreads();  // shared memory is reused by the next work item
+    // no barrier here: the next item's opening barrier orders this item's reads
+    // of shared memory before the next item's writes
   }
 }
 
