@@ -69,6 +69,9 @@ struct Geo2 {
 #ifndef OMHD_MIXED_TILE_Y
 #define OMHD_MIXED_TILE_Y 16
 #endif
+#ifndef OMHD_MIXED_MIN_CTAS  // resident CTAs per SM the FP32-mixed stage kernel is built for
+#define OMHD_MIXED_MIN_CTAS 2
+#endif
 template <class T>
 struct GeoFor {
   using type = Geo2<16, 16>;
@@ -711,7 +714,8 @@ __device__ __forceinline__ double stage2d_tile(const StageArgs& a, int bxi, int 
 
 // one CTA per tile of one grid
 template <class T, int FLUX, int TAPE = tape::kNone>
-__global__ void __launch_bounds__(GeoFor<T>::type::NT, sizeof(T) == 4 ? 2 : 1) k_stage2d(const StageArgs a) {
+__global__ void __launch_bounds__(GeoFor<T>::type::NT, sizeof(T) == 4 ? OMHD_MIXED_MIN_CTAS : 1)
+    k_stage2d(const StageArgs a) {
   using G = typename GeoFor<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red32[32];
