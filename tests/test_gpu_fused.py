@@ -193,8 +193,6 @@ def test_mixed_precision_error_vs_fp64(cuda_lib):
     assert np.all(err <= 1e-6), err
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("var,value,status", [(3, -5.0, 1), (4, -0.5, 2)])
 def test_mixed_precision_both_u2v_branches_vs_fp64(cuda_lib):
     """Orszag-Tang 256^2 with a 1.5x field (the batched set's strongest): the
     FP32-mixed path recovers the primitives in binary32 where the internal
@@ -221,6 +219,8 @@ def test_mixed_precision_both_u2v_branches_vs_fp64(cuda_lib):
     assert np.all(err <= 1e-6), err
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("var,value,status", [(3, -5.0, 1), (4, -0.5, 2)])
 def test_negative_pressure_is_reported_not_trapped(cuda_lib, precision, var, value, status):
     """E < 0 (negative pressure) or rho < 0 (negative density) in one cell is
     reported with the cell's Fortran index (u2v.f90:34-43), in FP64 and in the
