@@ -607,7 +607,7 @@ def run_batched(args, fp64_peak: float = float("nan"), fp32_peak: float = float(
             "members_stepping_throughout": active,
             "fp64_batched_value": updates64 / t64, "speedup_vs_fp64_batched": (updates / t) / (updates64 / t64),
             "cells": ens.cells, "precision": "mixed", "tile_kind": kind, "ctas_per_sm": cps,
-            "tile": ["32x8", "32x4", "16x16", "64x4"][kind], "ms_per_step": 1e3 * t / args.steps,
+            "tile": ["32x8", "32x4", "16x16", "64x4", "16x8"][kind], "ms_per_step": 1e3 * t / args.steps,
             "steps_compared": total_steps, "max_member_scaled_l1_vs_fp64": max(errs),
             "worst_member": int(np.argmax(errs)),
             "median_member_scaled_l1_vs_fp64": float(np.median(errs)),

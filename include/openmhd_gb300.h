@@ -332,7 +332,7 @@ int omhd_ensemble_set_stream(omhd_ensemble* e, void* cuda_stream);
 /* member i as a solver handle (state pointer, put/get state, coordinates) */
 int omhd_ensemble_member(omhd_ensemble* e, int i, omhd_solver** s);
 int omhd_ensemble_init_models(omhd_ensemble* e, const omhd_model* models);
-/* tile_kind 0: 32x8, 1: 32x4, 2: 16x16, 3: 64x4 cells per CTA; CTAs = ctas_per_sm x SMs */
+/* tile_kind 0: 32x8, 1: 32x4, 2: 16x16, 3: 64x4, 4: 16x8 cells per CTA; CTAs = ctas_per_sm x SMs */
 int omhd_ensemble_set_tiling(omhd_ensemble* e, int tile_kind, int ctas_per_sm);
 /* time `steps` real steps per candidate tiling, each from the same ensemble
  * state (saved and restored: tuning leaves the states, times and step counts

@@ -240,7 +240,7 @@ int omhd_ensemble_autotune(omhd_ensemble* e, int steps, int* best_kind, int* bes
   double best = 1e300;
   int bk = 0, bc = 1;
   for (int kind = 0; kind < kBatchTileKinds; ++kind)
-    for (int cps = 1; cps <= 2; ++cps) {
+    for (int cps = 1; cps <= batch_max_ctas(kind, e->precision == OMHD_PREC_MIXED); ++cps) {
       int r = omhd_ensemble_set_tiling(e, kind, cps);
       if (r) continue;
       r = omhd_ensemble_step(e, 1);  // warm-up: first launch configures the kernel

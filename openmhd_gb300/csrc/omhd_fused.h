@@ -46,17 +46,21 @@ int launch_stage2d_parity(const StageArgs& a, cudaStream_t s);
 int launch_stage2d_mixed(const StageArgs& a, cudaStream_t s);
 // fp64 HLLD stage with a decision tape: mode tape::kRecord or tape::kReplay
 int launch_stage2d_fp64_tape(const StageArgs& a, int mode, cudaStream_t s);
-// ensemble launchers: tile_kind 0: 32x8, 1: 32x4, 2: 16x16, 3: 64x4 cells per CTA
+// ensemble launchers: tile_kind 0: 32x8, 1: 32x4, 2: 16x16, 3: 64x4, 4: 16x8 cells per CTA
 int launch_batch2d_fp64(int flux, int tile_kind, const StageArgs* args_dev, int* tile_start_dev, int ngrids,
                         int total_tiles, int ctas, cudaStream_t s);
 int launch_batch2d_mixed(int flux, int tile_kind, const StageArgs* args_dev, int* tile_start_dev, int ngrids,
                          int total_tiles, int ctas, cudaStream_t s);
-constexpr int kBatchTileKinds = 4;
+constexpr int kBatchTileKinds = 5;
 inline void batch_tile_dims(int kind, int* tx, int* ty) {
-  static const int d[4][2] = {{32, 8}, {32, 4}, {16, 16}, {64, 4}};
-  *tx = d[kind & 3][0];
-  *ty = d[kind & 3][1];
+  static const int d[kBatchTileKinds][2] = {{32, 8}, {32, 4}, {16, 16}, {64, 4}, {16, 8}};
+  const int k = (kind >= 0 && kind < kBatchTileKinds) ? kind : 0;
+  *tx = d[k][0];
+  *ty = d[k][1];
 }
+// the most CTAs per SM a batched kernel of this tile kind is built for
+// (FP32-mixed: 160-thread tiles four, 288-thread tiles two; FP64: two)
+inline int batch_max_ctas(int kind, bool mixed) { return (mixed && (kind == 1 || kind == 4)) ? 4 : 2; }
 // Kernels with more than 48 KB of dynamic shared memory need the attribute
 // set on every device that launches them: once per (kernel, device), tracked
 // in the caller's bit mask (devices 0..63; beyond that, every launch sets it).

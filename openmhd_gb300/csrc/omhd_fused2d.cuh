@@ -58,19 +58,21 @@ struct Geo2 {
   }
   static_assert((NV * (RY * RX + 2 * (NXS + NYS))) % 2 == 0, "flux block must start 8-byte aligned");
 };
-// tile of the single-grid stage kernel per arithmetic type: 16x16, whose halo
-// is the smallest of the shapes a 288-thread CTA serves (1.5 loaded cells per
-// cell); the FP32-mixed kernel (two CTAs per SM) measured 16x16 / 32x8 / 64x4 at
-// 1.885e9 / 1.868e9 / 1.824e9 cell-updates/s on KH 4096x2048 (a build-time
-// constant, for tuning)
+// tile of the single-grid stage kernel per arithmetic type.  FP64: 16x16, whose
+// halo is the smallest of the shapes a 288-thread CTA serves (1.5 loaded cells
+// per cell).  FP32-mixed: 16x8 tiles of 160 threads, four CTAs per SM (96
+// registers): more CTAs interleave their barrier-separated phases; measured on
+// KH 4096x2048, 16x8 at 4 / 3 CTAs per SM and 16x16 / 32x8 / 64x4 at 2 CTAs per
+// SM gave 1.985e9 / 1.819e9 and 1.894e9 / 1.868e9 / 1.824e9 cell-updates/s
+// (build-time constants, for tuning)
 #ifndef OMHD_MIXED_TILE_X
 #define OMHD_MIXED_TILE_X 16
 #endif
 #ifndef OMHD_MIXED_TILE_Y
-#define OMHD_MIXED_TILE_Y 16
+#define OMHD_MIXED_TILE_Y 8
 #endif
 #ifndef OMHD_MIXED_MIN_CTAS  // resident CTAs per SM the FP32-mixed stage kernel is built for
-#define OMHD_MIXED_MIN_CTAS 2
+#define OMHD_MIXED_MIN_CTAS 4
 #endif
 template <class T>
 struct GeoFor {
@@ -927,10 +929,12 @@ int launch_pipe(const StageArgs& a, cudaStream_t s) {
 // cheap this step (finished, or failed) leave no CTA idle; each grid keeps its
 // own dt, step record and error word, and the CTA that finishes the last tile
 // of a grid in stage 2 plans that grid's next step.
-// FP32-mixed: two CTAs per SM (registers capped at 112 for 288 threads) hide
-// the latency of the FP64 load and update phases behind each other's work
+// FP32-mixed: two CTAs per SM for 288-thread tiles, four for 160-thread tiles
+// (96 registers), hide the latency of the FP64 load and update phases and of
+// the barriers behind each other's work
 template <class T, int FLUX, class G>
-__global__ void __launch_bounds__(G::NT, sizeof(T) == 4 ? 2 : 1) k_batch2d(const StageArgs* __restrict__ args,
+__global__ void __launch_bounds__(G::NT, sizeof(T) == 4 ? (G::NT <= 160 ? 4 : 2) : 1)
+    k_batch2d(const StageArgs* __restrict__ args,
                                                    const int* __restrict__ tile_start, int ngrids, int total_tiles,
                                                    int* __restrict__ queue) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1031,7 +1035,8 @@ int launch_batch_variant(int flux, int tile_kind, const StageArgs* args, int* ti
     case 0: return launch_batch_one<T, FX_HLLD, Geo2<32, 8>>(args, tile_start, ngrids, total_tiles, ctas, s);
     case 1: return launch_batch_one<T, FX_HLLD, Geo2<32, 4>>(args, tile_start, ngrids, total_tiles, ctas, s);
     case 2: return launch_batch_one<T, FX_HLLD, Geo2<16, 16>>(args, tile_start, ngrids, total_tiles, ctas, s);
-    default: return launch_batch_one<T, FX_HLLD, Geo2<64, 4>>(args, tile_start, ngrids, total_tiles, ctas, s);
+    case 3: return launch_batch_one<T, FX_HLLD, Geo2<64, 4>>(args, tile_start, ngrids, total_tiles, ctas, s);
+    default: return launch_batch_one<T, FX_HLLD, Geo2<16, 8>>(args, tile_start, ngrids, total_tiles, ctas, s);
   }
 }
 

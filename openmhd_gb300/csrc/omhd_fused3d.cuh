@@ -28,13 +28,18 @@ namespace d3 {
 constexpr int TX = 32, TY = 8, NT = TX * TY;
 constexpr int RX = TX + 4, RY = TY + 4, PL = RX * RY;  // plane of the halo tile
 constexpr int NRING = 4;
-constexpr int SFACE = (TY * (TX + 2) > (TY + 2) * TX) ? TY * (TX + 2) : (TY + 2) * TX;
-constexpr int SFLUX = (TY * (TX + 1) > (TY + 1) * TX) ? TY * (TX + 1) : (TY + 1) * TX;
+constexpr int XS = TX + 2, NXS3 = TY * XS;        // cells reconstructed in x (a row strip per tile row)
+constexpr int NYS3 = (TY + 2) * TX;               // cells reconstructed in y
+constexpr int XF = TX + 1, NXF3 = TY * XF;        // x faces
+constexpr int NXFP3 = (NXF3 + 31) / 32 * 32;      // x faces padded to whole warps
+constexpr int NYF3 = (TY + 1) * TX;               // y faces
 constexpr int ZCHUNK = 64;  // z planes marched by one CTA
 
+// ring of NRING primitive planes, then the x and y face states of one plane;
+// each face's flux overwrites the lower-cell face state that only it reads
 template <class T>
 constexpr size_t smem3d_bytes() {
-  return sizeof(T) * (size_t)NV * (NRING * PL + 2 * SFACE + SFLUX);
+  return sizeof(T) * (size_t)NV * (NRING * PL + 2 * NXS3 + 2 * NYS3);
 }
 
 __device__ __forceinline__ int map_idx(int g, int n, bool periodic) {
@@ -149,9 +154,10 @@ template <class T, int FLUX>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const StageArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* W = reinterpret_cast<T*>(smem_raw);  // [NRING][NV][PL]
-  T* SL = W + NRING * NV * PL;
-  T* SR = SL + NV * SFACE;
-  T* FB = SR + NV * SFACE;
+  T* SLx = W + NRING * NV * PL;  // [NV][NXS3]; x fluxes in place
+  T* SRx = SLx + NV * NXS3;
+  T* SLy = SRx + NV * NXS3;      // [NV][NYS3]; y fluxes in place
+  T* SRy = SLy + NV * NYS3;
   __shared__ double red32[32];
   __shared__ int skip;
 
@@ -255,7 +261,14 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
   double vloc = 0.0;
 
   for (int k = k0; k <= k1; ++k) {
-    __syncthreads();  // ring slot of plane k-2 is free
+    // Three CTA barriers per plane (plus one where a wall fix is needed).  The
+    // ring slot of plane k+2 held plane k-2, whose last readers (the resistive
+    // terms of plane k-1) finished before the previous plane's flux barrier;
+    // the face arrays are rewritten only after the barrier that follows this
+    // load, which every thread reaches after its reads of the previous plane's
+    // fluxes.  The prologue's z face reads plane k0-2: one barrier before the
+    // first load.
+    if (k == k0) __syncthreads();
     load_plane<T>(a, W, slot(k + 2), k + 2, gi0, gj0, perx, pery, perz, resist, glmf, false);
     __syncthreads();
     if (k > k0) {
@@ -271,149 +284,145 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
     }
     const T* Wk = W + (size_t)slot(k) * NV * PL;
 
-    // ---- x pass on plane k ----
-    constexpr int XS = TX + 2;
-    for (int q = tid; q < TY * XS; q += NT) {
-      const int cx = q % XS, cy = q / XS;
-      const int o = (cy + 2) * RX + (cx + 1);
+    // ---- x and y face states of plane k, one phase ----
+    for (int q = tid; q < NXS3 + NYS3; q += NT) {
+      const bool xd = q < NXS3;
+      const int qq = xd ? q : q - NXS3;
+      int o, st;
+      if (xd) {  // x row cy, cells cx = 0..TX+1 (tile columns -1..TX)
+        const int cx = qq % XS, cy = qq / XS;
+        o = (cy + 2) * RX + (cx + 1);
+        st = 1;
+      } else {  // y column cx, cells cy = 0..TY+1 (tile rows -1..TY)
+        const int cx = qq % TX, cy = qq / TX;
+        o = (cy + 1) * RX + (cx + 2);
+        st = RX;
+      }
+      T* dl = xd ? SLx : SLy;
+      T* dr = xd ? SRx : SRy;
+      const int sv = xd ? NXS3 : NYS3;
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
         T l, r;
-        reconstruct_t<T, OMHD_FAST>(lm, Wk[v * PL + o - 1], Wk[v * PL + o], Wk[v * PL + o + 1], l, r);
-        SL[v * SFACE + q] = l;
-        SR[v * SFACE + q] = r;
+        reconstruct_t<T, OMHD_FAST>(lm, Wk[v * PL + o - st], Wk[v * PL + o], Wk[v * PL + o + st], l, r);
+        dl[v * sv + qq] = l;
+        dr[v * sv + qq] = r;
       }
     }
     __syncthreads();
-    if (!perx) {
-      if (gi0 == 1 && tid < TY * NV) {
+    if (!perx || !pery) {  // wall face fixes, x by the first threads, y by the last
+      if (!perx && tid < TY * NV) {
         const int cy = tid % TY, v = tid / TY;
-        const T s = SR[v * SFACE + cy * XS + 1];
-        SL[v * SFACE + cy * XS + 0] = ((a.bc_flip[0] >> v) & 1) ? -s : s;
+        if (gi0 == 1) {
+          const T s = SRx[v * NXS3 + cy * XS + 1];
+          SLx[v * NXS3 + cy * XS + 0] = ((a.bc_flip[0] >> v) & 1) ? -s : s;
+        }
+        const int cl = (ix - 2) - gi0 + 1;
+        if (cl >= 1 && cl <= TX) {
+          const T s = SLx[v * NXS3 + cy * XS + cl];
+          SRx[v * NXS3 + cy * XS + cl + 1] = ((a.bc_flip[1] >> v) & 1) ? -s : s;
+        }
       }
-      const int cl = (ix - 2) - gi0 + 1;
-      if (cl >= 1 && cl <= TX && tid < TY * NV) {
-        const int cy = tid % TY, v = tid / TY;
-        const T s = SL[v * SFACE + cy * XS + cl];
-        SR[v * SFACE + cy * XS + cl + 1] = ((a.bc_flip[1] >> v) & 1) ? -s : s;
-      }
-      __syncthreads();
-    }
-    constexpr int XF = TX + 1;
-    for (int q = tid; q < TY * XF; q += NT) {
-      const int fx = q % XF, cy = q / XF;
-      T L[NV], R[NV], Fo[NV];
-#pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        L[v] = SL[v * SFACE + cy * XS + fx];
-        R[v] = SR[v * SFACE + cy * XS + fx + 1];
-      }
-      riemann_flux<T, 1, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
-      if (resist) {  // flux_resistive.cuf:87-101
-        const int g = gi0 - 1 + fx, gjj = gj0 + cy;
-        if (g >= 0 && g <= ix - 2 && gjj <= jx - 2) {
-          const int o = (cy + 2) * RX + (fx + 1);
-          if constexpr (sizeof(T) == 4) {
-            auto b = [&](int var, int dxo, int dyo, int dzo) { return Wv(k + dzo, var, o + dxo + dyo * RX); };
-            const float eta_dx = sep_eta ? harris_eta_dx<T>(ex_f[fx], ez_c[k - k0 + 1], inv_dx_t)
-                                         : narrow_f64(eta3(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gjj], a.zc[k]) / a.dx);
-            resist_face_f32<1>(b, eta_dx, Fo);
-          } else {
-            auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, o + dxo + dyo * RX)); };
-            const double eta_dx = sep_eta ? harris_eta_dx<double>(ex_f[fx], ez_c[k - k0 + 1], inv_dx)
-                                          : eta3(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gjj], a.zc[k]) / a.dx;
-            const double JyS = -(B(BZ, 1, 0, 0) - B(BZ, 0, 0, 0)) +
-                               0.25 * (B(BX, 0, 0, 1) + B(BX, 1, 0, 1) - B(BX, 0, 0, -1) - B(BX, 1, 0, -1));
-            const double JzS = (B(BY, 1, 0, 0) - B(BY, 0, 0, 0)) -
-                               0.25 * (B(BX, 0, 1, 0) + B(BX, 1, 1, 0) - B(BX, 0, -1, 0) - B(BX, 1, -1, 0));
-            Fo[EN] = Fo[EN] + 0.5 * eta_dx * (JyS * (B(BZ, 0, 0, 0) + B(BZ, 1, 0, 0)) - JzS * (B(BY, 0, 0, 0) + B(BY, 1, 0, 0)));
-            Fo[BY] = Fo[BY] - eta_dx * JzS;
-            Fo[BZ] = Fo[BZ] + eta_dx * JyS;
+      if (!pery && tid >= NT - TX) {
+        const int cx = tid - (NT - TX);
+        const int cl = (jx - 2) - gj0 + 1;
+        for (int v = 0; v < NV; ++v) {
+          if (gj0 == 1) {
+            const T s = SRy[v * NYS3 + 1 * TX + cx];
+            SLy[v * NYS3 + 0 * TX + cx] = ((a.bc_flip[2] >> v) & 1) ? -s : s;
+          }
+          if (cl >= 1 && cl <= TY) {
+            const T s = SLy[v * NYS3 + cl * TX + cx];
+            SRy[v * NYS3 + (cl + 1) * TX + cx] = ((a.bc_flip[3] >> v) & 1) ? -s : s;
           }
         }
       }
-#pragma unroll
-      for (int v = 0; v < NV; ++v) FB[v * SFLUX + q] = Fo[v];
+      __syncthreads();
     }
-    __syncthreads();
-    double acc[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v)
-      acc[v] = to_f64<T>(FB[v * SFLUX + ty * XF + tx]) - to_f64<T>(FB[v * SFLUX + ty * XF + tx + 1]);
-    // no barrier here: the y reconstruction writes only SL/SR (last read by the
-    // x fluxes, before the barrier above), and FB is next written by the y
-    // fluxes, after the barrier that follows the y reconstruction
 
-    // ---- y pass on plane k ----
-    for (int q = tid; q < (TY + 2) * TX; q += NT) {
-      const int cx = q % TX, cy = q / TX;
-      const int o = (cy + 1) * RX + (cx + 2);
+    // ---- x and y fluxes of plane k, one phase (x faces padded to whole
+    // warps, so that no warp mixes directions); each flux replaces the
+    // lower-cell face state that only its own face reads ----
+    for (int q = tid; q < NXFP3 + NYF3; q += NT) {
+      if (q < NXFP3) {
+        if (q >= NXF3) continue;  // padding lanes
+        const int fx = q % XF, cy = q / XF;
+        T L[NV], R[NV], Fo[NV];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        T l, r;
-        reconstruct_t<T, OMHD_FAST>(lm, Wk[v * PL + o - RX], Wk[v * PL + o], Wk[v * PL + o + RX], l, r);
-        SL[v * SFACE + q] = l;
-        SR[v * SFACE + q] = r;
-      }
-    }
-    __syncthreads();
-    if (!pery) {
-      if (gj0 == 1 && tid < TX) {
         for (int v = 0; v < NV; ++v) {
-          const T s = SR[v * SFACE + 1 * TX + tid];
-          SL[v * SFACE + 0 * TX + tid] = ((a.bc_flip[2] >> v) & 1) ? -s : s;
+          L[v] = SLx[v * NXS3 + cy * XS + fx];
+          R[v] = SRx[v * NXS3 + cy * XS + fx + 1];
         }
-      }
-      const int cl = (jx - 2) - gj0 + 1;
-      if (cl >= 1 && cl <= TY && tid < TX) {
-        for (int v = 0; v < NV; ++v) {
-          const T s = SL[v * SFACE + cl * TX + tid];
-          SR[v * SFACE + (cl + 1) * TX + tid] = ((a.bc_flip[3] >> v) & 1) ? -s : s;
-        }
-      }
-      __syncthreads();
-    }
-    for (int q = tid; q < (TY + 1) * TX; q += NT) {
-      const int cx = q % TX, fy = q / TX;
-      T L[NV], R[NV], Fo[NV];
-#pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        L[v] = SL[v * SFACE + fy * TX + cx];
-        R[v] = SR[v * SFACE + (fy + 1) * TX + cx];
-      }
-      riemann_flux<T, 2, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
-      if (resist) {  // flux_resistive.cuf:104-118
-        const int gii = gi0 + cx, g = gj0 - 1 + fy;
-        if (g >= 0 && g <= jx - 2 && gii <= ix - 2) {
-          const int o = (fy + 1) * RX + (cx + 2);
-          if constexpr (sizeof(T) == 4) {
-            auto b = [&](int var, int dxo, int dyo, int dzo) { return Wv(k + dzo, var, o + dxo + dyo * RX); };
-            const float eta_dx = sep_eta ? harris_eta_dx<T>(ex_c[cx + 1], ez_c[k - k0 + 1], inv_dx_t)
-                                         : narrow_f64(eta3(a.eta_kind, a.xc[gii], a.yc[g] + 0.5 * a.dx, a.zc[k]) / a.dx);
-            resist_face_f32<2>(b, eta_dx, Fo);
-          } else {
-            auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, o + dxo + dyo * RX)); };
-            const double eta_dx = sep_eta ? harris_eta_dx<double>(ex_c[cx + 1], ez_c[k - k0 + 1], inv_dx)
-                                          : eta3(a.eta_kind, a.xc[gii], a.yc[g] + 0.5 * a.dx, a.zc[k]) / a.dx;
-            const double JxS = (B(BZ, 0, 1, 0) - B(BZ, 0, 0, 0)) -
-                               0.25 * (B(BY, 0, 0, 1) + B(BY, 0, 1, 1) - B(BY, 0, 0, -1) - B(BY, 0, 1, -1));
-            const double JzS = -(B(BX, 0, 1, 0) - B(BX, 0, 0, 0)) +
-                               0.25 * (B(BY, 1, 0, 0) + B(BY, 1, 1, 0) - B(BY, -1, 0, 0) - B(BY, -1, 1, 0));
-            Fo[EN] = Fo[EN] + 0.5 * eta_dx * (JzS * (B(BX, 0, 0, 0) + B(BX, 0, 1, 0)) - JxS * (B(BZ, 0, 0, 0) + B(BZ, 0, 1, 0)));
-            Fo[BX] = Fo[BX] + eta_dx * JzS;
-            Fo[BZ] = Fo[BZ] - eta_dx * JxS;
+        riemann_flux<T, 1, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
+        if (resist) {  // flux_resistive.cuf:87-101
+          const int g = gi0 - 1 + fx, gjj = gj0 + cy;
+          if (g >= 0 && g <= ix - 2 && gjj <= jx - 2) {
+            const int o = (cy + 2) * RX + (fx + 1);
+            if constexpr (sizeof(T) == 4) {
+              auto b = [&](int var, int dxo, int dyo, int dzo) { return Wv(k + dzo, var, o + dxo + dyo * RX); };
+              const float eta_dx = sep_eta ? harris_eta_dx<T>(ex_f[fx], ez_c[k - k0 + 1], inv_dx_t)
+                                           : narrow_f64(eta3(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gjj], a.zc[k]) / a.dx);
+              resist_face_f32<1>(b, eta_dx, Fo);
+            } else {
+              auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, o + dxo + dyo * RX)); };
+              const double eta_dx = sep_eta ? harris_eta_dx<double>(ex_f[fx], ez_c[k - k0 + 1], inv_dx)
+                                            : eta3(a.eta_kind, a.xc[g] + 0.5 * a.dx, a.yc[gjj], a.zc[k]) / a.dx;
+              const double JyS = -(B(BZ, 1, 0, 0) - B(BZ, 0, 0, 0)) +
+                                 0.25 * (B(BX, 0, 0, 1) + B(BX, 1, 0, 1) - B(BX, 0, 0, -1) - B(BX, 1, 0, -1));
+              const double JzS = (B(BY, 1, 0, 0) - B(BY, 0, 0, 0)) -
+                                 0.25 * (B(BX, 0, 1, 0) + B(BX, 1, 1, 0) - B(BX, 0, -1, 0) - B(BX, 1, -1, 0));
+              Fo[EN] = Fo[EN] + 0.5 * eta_dx * (JyS * (B(BZ, 0, 0, 0) + B(BZ, 1, 0, 0)) - JzS * (B(BY, 0, 0, 0) + B(BY, 1, 0, 0)));
+              Fo[BY] = Fo[BY] - eta_dx * JzS;
+              Fo[BZ] = Fo[BZ] + eta_dx * JyS;
+            }
           }
         }
-      }
 #pragma unroll
-      for (int v = 0; v < NV; ++v) FB[v * SFLUX + q] = Fo[v];
+        for (int v = 0; v < NV; ++v) SLx[v * NXS3 + cy * XS + fx] = Fo[v];
+      } else {
+        const int qq = q - NXFP3;
+        const int cx = qq % TX, fy = qq / TX;
+        T L[NV], R[NV], Fo[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          L[v] = SLy[v * NYS3 + fy * TX + cx];
+          R[v] = SRy[v * NYS3 + (fy + 1) * TX + cx];
+        }
+        riemann_flux<T, 2, FLUX, OMHD_FAST>(L, R, ch, gam, r1, r2, Fo);
+        if (resist) {  // flux_resistive.cuf:104-118
+          const int gii = gi0 + cx, g = gj0 - 1 + fy;
+          if (g >= 0 && g <= jx - 2 && gii <= ix - 2) {
+            const int o = (fy + 1) * RX + (cx + 2);
+            if constexpr (sizeof(T) == 4) {
+              auto b = [&](int var, int dxo, int dyo, int dzo) { return Wv(k + dzo, var, o + dxo + dyo * RX); };
+              const float eta_dx = sep_eta ? harris_eta_dx<T>(ex_c[cx + 1], ez_c[k - k0 + 1], inv_dx_t)
+                                           : narrow_f64(eta3(a.eta_kind, a.xc[gii], a.yc[g] + 0.5 * a.dx, a.zc[k]) / a.dx);
+              resist_face_f32<2>(b, eta_dx, Fo);
+            } else {
+              auto B = [&](int var, int dxo, int dyo, int dzo) { return to_f64<T>(Wv(k + dzo, var, o + dxo + dyo * RX)); };
+              const double eta_dx = sep_eta ? harris_eta_dx<double>(ex_c[cx + 1], ez_c[k - k0 + 1], inv_dx)
+                                            : eta3(a.eta_kind, a.xc[gii], a.yc[g] + 0.5 * a.dx, a.zc[k]) / a.dx;
+              const double JxS = (B(BZ, 0, 1, 0) - B(BZ, 0, 0, 0)) -
+                                 0.25 * (B(BY, 0, 0, 1) + B(BY, 0, 1, 1) - B(BY, 0, 0, -1) - B(BY, 0, 1, -1));
+              const double JzS = -(B(BX, 0, 1, 0) - B(BX, 0, 0, 0)) +
+                                 0.25 * (B(BY, 1, 0, 0) + B(BY, 1, 1, 0) - B(BY, -1, 0, 0) - B(BY, -1, 1, 0));
+              Fo[EN] = Fo[EN] + 0.5 * eta_dx * (JzS * (B(BX, 0, 0, 0) + B(BX, 0, 1, 0)) - JxS * (B(BZ, 0, 0, 0) + B(BZ, 0, 1, 0)));
+              Fo[BX] = Fo[BX] + eta_dx * JzS;
+              Fo[BZ] = Fo[BZ] - eta_dx * JxS;
+            }
+          }
+        }
+#pragma unroll
+        for (int v = 0; v < NV; ++v) SLy[v * NYS3 + fy * TX + cx] = Fo[v];
+      }
     }
     __syncthreads();
-    double gm[NV], gp[NV];
+    double acc[NV], gm[NV], gp[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      gm[v] = to_f64<T>(FB[v * SFLUX + ty * TX + tx]);
-      gp[v] = to_f64<T>(FB[v * SFLUX + (ty + 1) * TX + tx]);
+      acc[v] = to_f64<T>(SLx[v * NXS3 + ty * XS + tx]) - to_f64<T>(SLx[v * NXS3 + ty * XS + tx + 1]);
+      gm[v] = to_f64<T>(SLy[v * NYS3 + ty * TX + tx]);
+      gp[v] = to_f64<T>(SLy[v * NYS3 + (ty + 1) * TX + tx]);
     }
 
     // ---- z face k+1/2 in registers ----
