@@ -975,11 +975,11 @@ def run_profile(args):
 
     from openmhd_gb300 import Solver, harris3d, kelvin_helmholtz
 
-    if args.one_role_3d or args.one_role_2d:
+    if args.pipelined_3d or args.one_role_2d:
         from openmhd_gb300 import _lib
 
-        if args.one_role_3d:
-            _lib.load().omhd_set_3d_pipeline(0)
+        if args.pipelined_3d:
+            _lib.load().omhd_set_3d_pipeline(1)
         if args.one_role_2d:
             _lib.load().omhd_set_2d_pipeline(0)
     if args.nz:
@@ -1088,8 +1088,8 @@ def main():
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--nz", type=int, default=0)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_parity", "mixed"])
-    ap.add_argument("--one-role-3d", action="store_true",
-                    help="with --profile: the one-role FP64 3D stage kernel instead of the warp-specialised one")
+    ap.add_argument("--pipelined-3d", action="store_true",
+                    help="with --profile: the warp-specialised FP64 3D stage kernel instead of the one-role one")
     ap.add_argument("--one-role-2d", action="store_true",
                     help="with --profile: the one-role 2D stage kernels instead of the warp-specialised ones")
     ap.add_argument("--accuracy", action="store_true",

@@ -207,9 +207,10 @@ int omhd_probe_fp64_peak(double* gflops);
  * Library-global: set it before stepping, from one thread. */
 void omhd_set_tma_staging(int enable);
 /* The warp-specialised FP64 3D stage kernel (HLLD with minmod or MC; no
- * counterpart in the reference): on by default; 0 selects the one-role 3D
- * kernel (same scheme; results agree to rounding), for comparisons.
- * Library-global: set it before stepping, from one thread. */
+ * counterpart in the reference): off by default, where the one-role 3D kernel
+ * runs (three CTA barriers per plane; the faster of the two on GB300); 1
+ * selects the warp-specialised kernel (same scheme; results agree to
+ * rounding).  Library-global: set it before stepping, from one thread. */
 void omhd_set_3d_pipeline(int enable);
 /* The warp-specialised FP64 2D stage kernel (HLLD with minmod or MC, no
  * resistivity; no counterpart in the reference): on by default; 0 selects the

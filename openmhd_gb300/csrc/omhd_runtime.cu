@@ -199,7 +199,7 @@ __global__ void k_convert_probe(const double* __restrict__ xd, float* __restrict
 
 static std::atomic<int> g_tma_on{1};
 bool tma_staging_enabled() { return g_tma_on.load(std::memory_order_relaxed) != 0; }
-static std::atomic<int> g_pipe3d_on{1};
+static std::atomic<int> g_pipe3d_on{0};
 bool pipe3d_enabled() { return g_pipe3d_on.load(std::memory_order_relaxed) != 0; }
 static std::atomic<int> g_pipe2d_on{1};
 bool pipe2d_enabled() { return g_pipe2d_on.load(std::memory_order_relaxed) != 0; }

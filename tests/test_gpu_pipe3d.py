@@ -1,7 +1,8 @@
 """The warp-specialised FP64 3D stage kernel (k_stage3d_pipe: 3 producer warps
 build the ring planes and the x / y / z face states of the next plane while 9
-consumer warps solve the faces and update the current one) against the oracle
-and against the one-role 3D kernel (omhd_set_3d_pipeline(0)).
+consumer warps solve the faces and update the current one; selected by
+omhd_set_3d_pipeline(1), the one-role kernel being the default) against the
+oracle and against the one-role 3D kernel.
 
 The two kernels do the same arithmetic except that the pipelined one solves y
 and z faces in x orientation (the component order of sums such as B^2
@@ -12,6 +13,15 @@ import pytest
 from helpers import assert_parity, random_state, scaled_l1
 
 pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def _pipelined(cuda_lib):
+    """Every test here runs the warp-specialised kernel unless it says
+    otherwise; the library default (the one-role kernel) is put back after."""
+    cuda_lib.omhd_set_3d_pipeline(1)
+    yield
+    cuda_lib.omhd_set_3d_pipeline(0)
 
 
 def _oracle_pair(cfg, model=None, U=None):
