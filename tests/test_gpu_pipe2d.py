@@ -6,10 +6,10 @@ than the GPU has SMs (every CTA runs several tiles through both buffers),
 ragged edge tiles, walls and periodic edges; the two kernels compute the same
 expressions and agree to FP64 rounding (scaled L1 <= 1e-13 after 4 steps).
 
-The FP32-mixed path keeps the one-role kernel at two CTAs per SM: a
+The FP32-mixed path keeps one-role kernels (four 16x8-tile CTAs per SM): a
 pipelined FP32-mixed variant (4 producer + 9 consumer warps, 32x8 tiles, and
 variants with 2 or 6 producer warps and 32x12 or 32x16 tiles) ran 3-11 %
-slower on KH 4096x2048."""
+slower than the one-role kernel of the time on KH 4096x2048."""
 import numpy as np
 import pytest
 
