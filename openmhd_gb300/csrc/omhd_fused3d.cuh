@@ -25,7 +25,15 @@ namespace omhd {
 namespace OMHD_VARIANT {
 namespace d3 {
 
-constexpr int TX = 32, TY = 8, NT = TX * TY;
+// column of the one-role kernel (build-time constants, for tuning)
+#ifndef OMHD_3D_TILE_X
+#define OMHD_3D_TILE_X 32
+#endif
+#ifndef OMHD_3D_TILE_Y
+#define OMHD_3D_TILE_Y 8
+#endif
+constexpr int TX = OMHD_3D_TILE_X, TY = OMHD_3D_TILE_Y, NT = TX * TY;
+static_assert(TY * NV <= NT - TX, "the x and y wall fixes use disjoint threads");
 constexpr int RX = TX + 4, RY = TY + 4, PL = RX * RY;  // plane of the halo tile
 constexpr int NRING = 4;
 constexpr int XS = TX + 2, NXS3 = TY * XS;        // cells reconstructed in x (a row strip per tile row)
