@@ -38,7 +38,25 @@ struct StageArgs {
   // stage 2 of the last step of omhd_solver_step_host: the result is also
   // written here (the device address of page-locked host memory), else nullptr
   double* Uhost;
+  // derived on the host by stage_args_derived (the 2D stage kernels read them
+  // instead of dividing in every CTA): dtx_scale/dx, dtx_scale/dy;
+  // 1/(gamma-1), gamma/(gamma-1) (flux_solver.f90:38-39) in FP64 and, with
+  // gamma, rounded to binary32 for the FP32 face arithmetic
+  double sdx, sdy;
+  double r1, r2;
+  float gamma_f, r1_f, r2_f;
 };
+
+// fills the derived fields of a once dx, dy, dtx_scale and gamma are set
+inline void stage_args_derived(StageArgs& a) {
+  a.sdx = a.dtx_scale / a.dx;
+  a.sdy = a.dtx_scale / a.dy;
+  a.r1 = 1.0 / (a.gamma - 1.0);
+  a.r2 = a.gamma / (a.gamma - 1.0);
+  a.gamma_f = (float)a.gamma;
+  a.r1_f = (float)a.r1;
+  a.r2_f = (float)a.r2;
+}
 
 // launchers: return 0 or a CUDA error code
 int launch_stage2d_fp64(const StageArgs& a, cudaStream_t s);

@@ -132,11 +132,14 @@ struct TileMem {
   int fxv, fxr, fyv;
 };
 
-// Scalars of one stage that each thread would otherwise derive itself (four
-// FP64 divisions per thread and tile, and for FP32 face arithmetic four
-// conversions): one thread computes them per CTA -- per work item in an
-// ensemble -- into shared memory, and the others read them after the next
-// CTA barrier.  Same expressions, so the same bits.
+// Scalars of one stage: one thread gathers them per CTA -- per work item in an
+// ensemble -- into shared memory, and the others read them after the next CTA
+// barrier.  The constant ones come derived from the host (stage_args_derived);
+// dt/dx is dt * (dtx_scale/dx) in the FAST builds (an FP64 division, a dozen
+// FP64-pipe instructions that one thread issues as whole warp instructions,
+// was 5-10 % of the FP32-mixed kernel's FP64 pipe time at 128 cells per CTA;
+// the product is within an ulp of the quotient) and the reference's
+// dtx_scale * dt / dx in the parity build.
 template <class T>
 struct StageScalars {
   double glmf;        // GLM damping factor of the step (glm_ss2.f90:27)
@@ -145,14 +148,25 @@ struct StageScalars {
 };
 template <class T>
 __device__ __forceinline__ void stage_scalars(const StageArgs& a, const StepState* st, StageScalars<T>& k) {
-  const double dt = st->dt, g = a.gamma;
+  const double dt = st->dt;
   k.glmf = st->glm_f;
-  k.dtx = a.dtx_scale * dt / a.dx;
-  k.dty = a.dtx_scale * dt / a.dy;
-  k.ch = T(st->ch);
-  k.gam = T(g);
-  k.r1 = T(1.0 / (g - 1.0));
-  k.r2 = T(g / (g - 1.0));
+  if constexpr (OMHD_FAST) {
+    k.dtx = dt * a.sdx;
+    k.dty = dt * a.sdy;
+  } else {
+    k.dtx = a.dtx_scale * dt / a.dx;
+    k.dty = a.dtx_scale * dt / a.dy;
+  }
+  k.ch = to_face<T>(st->ch);
+  if constexpr (sizeof(T) == 4) {
+    k.gam = a.gamma_f;
+    k.r1 = a.r1_f;
+    k.r2 = a.r2_f;
+  } else {
+    k.gam = a.gamma;
+    k.r1 = a.r1;
+    k.r2 = a.r2;
+  }
 }
 
 template <class T, class G>

@@ -285,6 +285,7 @@ int omhd_step2d_noalloc(double* U, const omhd_config* cfg, double t0, int nsteps
       a.U1 = (stage == 2) ? U1 : nullptr;
       a.Uout = (stage == 1) ? U1 : U;
       a.dtx_scale = (stage == 1 && cfg->time_type == OMHD_TIME_RK2) ? 0.5 : 1.0;
+      stage_args_derived(a);
       const int e = launch(a, s);
       if (e) return cuda_status((cudaError_t)e, "no-alloc stage kernel");
     }

@@ -274,6 +274,7 @@ StageArgs make_stage_args(const omhd_solver* s, int stage) {
   a.err = s->err;
   a.cfl = c.cfl;
   a.dmin = s->dmin;
+  stage_args_derived(a);
   return a;
 }
 }  // namespace omhd
