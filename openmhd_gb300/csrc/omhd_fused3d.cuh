@@ -528,9 +528,14 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
         const double B2 = out[BX] * out[BX] + out[BY] * out[BY] + out[BZ] * out[BZ];
         const double pr = f1g * (out[EN] - 0.5 * (rv2 + B2));
         const double f1 = gamma * pr;
-        double s = fmax2(fabs(vx) + fast_speed<double, OMHD_FAST>(f1, B2, out[BX], ro), fabs(vy) + fast_speed<double, OMHD_FAST>(f1, B2, out[BY], ro));
-        s = fmax2(s, fabs(vz) + fast_speed<double, OMHD_FAST>(f1, B2, out[BZ], ro));
-        vloc = fmax2(s, vloc);
+        // fmax2 of the three speeds and of the running max, the comparisons on
+        // the integer pipe in the FAST builds (same results)
+        const double sx = fabs(vx) + fast_speed<double, OMHD_FAST>(f1, B2, out[BX], ro);
+        const double sy = fabs(vy) + fast_speed<double, OMHD_FAST>(f1, B2, out[BY], ro);
+        const double sz = fabs(vz) + fast_speed<double, OMHD_FAST>(f1, B2, out[BZ], ro);
+        double s = lt_<double, OMHD_FAST>(sx, sy) ? sy : sx;
+        s = lt_<double, OMHD_FAST>(s, sz) ? sz : s;
+        vloc = lt_<double, OMHD_FAST>(s, vloc) ? vloc : s;
       }
     }
 #pragma unroll

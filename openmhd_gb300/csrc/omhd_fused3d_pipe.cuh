@@ -511,10 +511,14 @@ __global__ void __launch_bounds__(NTOT, 1) k_stage3d_pipe(const StageArgs a) {
           const double B2 = out[BX] * out[BX] + out[BY] * out[BY] + out[BZ] * out[BZ];
           const double pr = f1g * (out[EN] - 0.5 * (rv2 + B2));
           const double f1 = gamma * pr;
-          double s = fmax2(fabs(vx) + fast_speed<double, true>(f1, B2, out[BX], ro),
-                           fabs(vy) + fast_speed<double, true>(f1, B2, out[BY], ro));
-          s = fmax2(s, fabs(vz) + fast_speed<double, true>(f1, B2, out[BZ], ro));
-          vmax = fmax2(s, vmax);
+          // fmax2 of the three speeds and of the running max, compared on the
+          // integer pipe (same results)
+          const double sx = fabs(vx) + fast_speed<double, true>(f1, B2, out[BX], ro);
+          const double sy = fabs(vy) + fast_speed<double, true>(f1, B2, out[BY], ro);
+          const double sz = fabs(vz) + fast_speed<double, true>(f1, B2, out[BZ], ro);
+          double s = lt_<double, true>(sx, sy) ? sy : sx;
+          s = lt_<double, true>(s, sz) ? sz : s;
+          vmax = lt_<double, true>(s, vmax) ? vmax : s;
         }
       }
       if (i + 2 < nplanes) {  // the producers refill buffer b for plane p+2

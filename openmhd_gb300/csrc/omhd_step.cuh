@@ -69,20 +69,26 @@ __device__ __forceinline__ void finalize_step(StepState* s, const StepConsts& c,
   plan_next_step(s, c, vmax, err);
 }
 
-// warp + block max of non-negative doubles; result valid in thread 0
+// warp + block max of non-negative doubles; result valid in thread 0.  For
+// non-negative doubles the integer order of the bit patterns is the numeric
+// order, so the max runs on the integer pipe (a floating-point compare holds
+// the FP64 pipe like an FMA, and this reduction runs once per tile); a NaN
+// counts as 0.
 __device__ __forceinline__ double block_max_pos(double v, double* red32) {
+  long long b = __double_as_longlong(v);
+  if (b > 0x7ff0000000000000LL) b = 0;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmax2(v, __shfl_xor_sync(0xffffffffu, v, o));
+  for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   __syncthreads();
-  if (lane == 0) red32[w] = v;
+  if (lane == 0) red32[w] = __longlong_as_double(b);
   __syncthreads();
   if (w == 0) {
-    v = (lane < (int)(blockDim.x >> 5)) ? red32[lane] : 0.0;
+    b = (lane < (int)(blockDim.x >> 5)) ? __double_as_longlong(red32[lane]) : 0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax2(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
   }
-  return v;
+  return __longlong_as_double(b);
 }
 
 // Last-CTA-done pattern: every CTA publishes its max, the last to arrive
