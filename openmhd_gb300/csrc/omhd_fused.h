@@ -43,17 +43,19 @@ struct StageArgs {
   // 1/(gamma-1), gamma/(gamma-1) (flux_solver.f90:38-39) in FP64 and, with
   // gamma, rounded to binary32 for the FP32 face arithmetic
   double sdx, sdy;
-  double r1, r2;
-  float gamma_f, r1_f, r2_f;
+  double gm1, r1, r2;  // gamma - 1 (u2v.f90:11), 1/(gamma-1), gamma/(gamma-1)
+  float gamma_f, gm1_f, r1_f, r2_f;
 };
 
 // fills the derived fields of a once dx, dy, dtx_scale and gamma are set
 inline void stage_args_derived(StageArgs& a) {
   a.sdx = a.dtx_scale / a.dx;
   a.sdy = a.dtx_scale / a.dy;
+  a.gm1 = a.gamma - 1.0;
   a.r1 = 1.0 / (a.gamma - 1.0);
   a.r2 = a.gamma / (a.gamma - 1.0);
   a.gamma_f = (float)a.gamma;
+  a.gm1_f = (float)a.gm1;
   a.r1_f = (float)a.r1;
   a.r2_f = (float)a.r2;
 }

@@ -198,8 +198,8 @@ __device__ __forceinline__ void phase_load(const StageArgs& a, int bxi, int byi,
   const int gi0 = 1 + bxi * TX, gj0 = 1 + byi * TY;
   const bool perx = a.bc_kind[0] == OMHD_BC_PERIODIC, pery = a.bc_kind[2] == OMHD_BC_PERIODIC;
   const bool resist = a.eta_kind != OMHD_ETA_NONE;
-  const double f1g = a.gamma - 1;  // u2v.f90:11
-  const float f1g32 = sizeof(T) == 4 ? narrow_f64(f1g) : 0.0f;
+  const double f1g = a.gm1;  // u2v.f90:11, derived on the host
+  const float f1g32 = a.gm1_f;
   T* W = m.W;
   // FP64: two cells per pass, both cells' loads issued before either is
   // converted, so their global-memory latencies overlap; FP32-mixed (two CTAs
@@ -626,7 +626,7 @@ __device__ __forceinline__ double phase_update(const StageArgs& a, int bxi, int 
   const int gi0 = 1 + bxi * TX, gj0 = 1 + byi * TY;
   const bool perx = a.bc_kind[0] == OMHD_BC_PERIODIC, pery = a.bc_kind[2] == OMHD_BC_PERIODIC;
   const double gamma = a.gamma;
-  const double f1g = gamma - 1;
+  const double f1g = a.gm1;
   // the argument block may live in global memory (ensembles), where a store to
   // the state could alias it: every pointer and scalar used in the loop is
   // read once, here

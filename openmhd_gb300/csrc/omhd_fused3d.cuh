@@ -124,8 +124,8 @@ __device__ __forceinline__ void load_plane(const StageArgs& a, T* W, int slot, i
                                            bool pery, bool perz, bool resist, double glmf, bool own_plane) {
   const int ix = a.ix, jx = a.jx, kx = a.kx;
   const size_t N = (size_t)ix * jx * kx;
-  const double f1g = a.gamma - 1;
-  const float f1g32 = sizeof(T) == 4 ? narrow_f64(f1g) : 0.0f;
+  const double f1g = a.gm1;  // derived on the host
+  const float f1g32 = a.gm1_f;
   const int mk = map_idx(gk, kx, perz);
   T* Ws = W + (size_t)slot * NV * PL;
   for (int q = threadIdx.x; q < PL; q += NT) {
