@@ -889,21 +889,21 @@ def run_accuracy(args):
         return out
 
     marks2 = sorted({10, 100, 500, 1000, args.accuracy_steps})
-    marks3 = sorted({10, 100, 300, args.accuracy_steps_3d})
+    marks3 = sorted({10, 100, 300, max(args.accuracy_steps_3d, 1)})
     kh = lambda p: kelvin_helmholtz(NX, NY, precision=p)  # noqa: E731
     h3 = lambda p: harris3d(H3_NX, H3_NY, H3_NZ, precision=p)  # noqa: E731
-    res = {"accuracy": {
-        "kh2d_4096x2048": curve(kh, args.accuracy_steps, marks2),
-        "harris3d_512x256x512": curve(h3, args.accuracy_steps_3d, marks3),
-    }}
+    res = {"accuracy": {"kh2d_4096x2048": curve(kh, args.accuracy_steps, marks2)}}
+    if args.accuracy_steps_3d > 0:  # 0 skips the 3D run
+        res["accuracy"]["harris3d_512x256x512"] = curve(h3, args.accuracy_steps_3d, marks3)
     if args.accuracy_control:
         # control: the FP64 build against the FP64 build without multiply-add
         # contraction, i.e. how far round-off alone (1e-16 per operation) is
         # carried by the flow over the same steps
         res["accuracy"]["control_kh2d_fp64_vs_fp64_parity"] = curve(kh, args.accuracy_steps, marks2,
                                                                     ("fp64_parity", "fp64"))
-        res["accuracy"]["control_harris3d_fp64_vs_fp64_parity"] = curve(
-            h3, min(args.accuracy_steps_3d, 300), sorted({10, 100, 300}), ("fp64_parity", "fp64"))
+        if args.accuracy_steps_3d > 0:
+            res["accuracy"]["control_harris3d_fp64_vs_fp64_parity"] = curve(
+                h3, min(args.accuracy_steps_3d, 300), sorted({10, 100, 300}), ("fp64_parity", "fp64"))
     res["accuracy"]["ensemble_worst_members"] = _ensemble_worst_members(curve, args.accuracy_control)
     print(json.dumps(res), flush=True)
     return 0
@@ -1096,7 +1096,7 @@ def main():
     ap.add_argument("--accuracy", action="store_true",
                     help="long-run error of the FP32-mixed path against FP64 (KH 2D and Harris 3D)")
     ap.add_argument("--accuracy-steps", type=int, default=2000)
-    ap.add_argument("--accuracy-steps-3d", type=int, default=1000)
+    ap.add_argument("--accuracy-steps-3d", type=int, default=1000, help="0 skips the 3D run")
     ap.add_argument("--accuracy-control", action="store_true",
                     help="with --accuracy: also FP64 against FP64 without contraction (round-off growth)")
     args = ap.parse_args()
