@@ -135,11 +135,11 @@ struct TileMem {
 // Scalars of one stage: one thread gathers them per CTA -- per work item in an
 // ensemble -- into shared memory, and the others read them after the next CTA
 // barrier.  The constant ones come derived from the host (stage_args_derived);
-// dt/dx is dt * (dtx_scale/dx) in the FAST builds (an FP64 division, a dozen
-// FP64-pipe instructions that one thread issues as whole warp instructions,
-// was 5-10 % of the FP32-mixed kernel's FP64 pipe time at 128 cells per CTA;
-// the product is within an ulp of the quotient) and the reference's
-// dtx_scale * dt / dx in the parity build.
+// dt/dx is dt * (dtx_scale/dx) in the FAST builds (the FP64 divisions one
+// thread made here, before the barrier the CTA's other threads wait at, cost
+// 11 % of the FP32-mixed kernel's time at 128 cells per CTA; the product is
+// within an ulp of the quotient) and the reference's dtx_scale * dt / dx in the
+// parity build.
 template <class T>
 struct StageScalars {
   double glmf;        // GLM damping factor of the step (glm_ss2.f90:27)
