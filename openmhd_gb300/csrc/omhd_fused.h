@@ -38,11 +38,11 @@ struct StageArgs {
   // stage 2 of the last step of omhd_solver_step_host: the result is also
   // written here (the device address of page-locked host memory), else nullptr
   double* Uhost;
-  // derived on the host by stage_args_derived (the 2D stage kernels read them
-  // instead of dividing in every CTA): dtx_scale/dx, dtx_scale/dy;
+  // derived on the host by stage_args_derived (the stage kernels read them
+  // instead of dividing in every CTA): dtx_scale/dx, /dy, /dz;
   // 1/(gamma-1), gamma/(gamma-1) (flux_solver.f90:38-39) in FP64 and, with
   // gamma, rounded to binary32 for the FP32 face arithmetic
-  double sdx, sdy;
+  double sdx, sdy, sdz;
   double gm1, r1, r2;  // gamma - 1 (u2v.f90:11), 1/(gamma-1), gamma/(gamma-1)
   float gamma_f, gm1_f, r1_f, r2_f;
 };
@@ -51,6 +51,7 @@ struct StageArgs {
 inline void stage_args_derived(StageArgs& a) {
   a.sdx = a.dtx_scale / a.dx;
   a.sdy = a.dtx_scale / a.dy;
+  a.sdz = a.dtx_scale / a.dz;
   a.gm1 = a.gamma - 1.0;
   a.r1 = 1.0 / (a.gamma - 1.0);
   a.r2 = a.gamma / (a.gamma - 1.0);

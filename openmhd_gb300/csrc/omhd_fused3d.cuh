@@ -185,15 +185,29 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const St
   const bool perz = a.bc_kind[4] == OMHD_BC_PERIODIC;
   const bool resist = a.eta_kind != OMHD_ETA_NONE;
   const double gamma = a.gamma;
-  const double f1g = gamma - 1;
-  const T ch = T(chd), gam = T(gamma);
-  const T r1 = T(1.0 / (gamma - 1.0)), r2 = T(gamma / (gamma - 1.0));
+  // gamma constants derived on the host (stage_args_derived)
+  const double f1g = a.gm1;
+  const T ch = to_face<T>(chd);
+  T gam, r1, r2;
+  if constexpr (sizeof(T) == 4) {
+    gam = a.gamma_f;
+    r1 = a.r1_f;
+    r2 = a.r2_f;
+  } else {
+    gam = gamma;
+    r1 = a.r1;
+    r2 = a.r2;
+  }
   const int lm = a.lm_type;
   const int tx = tid % TX, ty = tid / TX;
   const int gi = gi0 + tx, gj = gj0 + ty;
   const bool own = gi <= ix - 2 && gj <= jx - 2;
   const int oc = (ty + 2) * RX + (tx + 2);  // own column in a ring plane
-  const double dtx = a.dtx_scale * dt / a.dx, dty = a.dtx_scale * dt / a.dy, dtz = a.dtx_scale * dt / a.dz;
+  // dt/dx as dt * (dtx_scale/dx) in the FAST builds (within an ulp), the
+  // reference's division in the parity build
+  const double dtx = OMHD_FAST ? dt * a.sdx : a.dtx_scale * dt / a.dx;
+  const double dty = OMHD_FAST ? dt * a.sdy : a.dtx_scale * dt / a.dy;
+  const double dtz = OMHD_FAST ? dt * a.sdz : a.dtx_scale * dt / a.dz;
   auto slot = [](int k) { return ((k % NRING) + NRING) % NRING; };
   auto Wv = [&](int k, int v, int o) -> T { return W[(size_t)slot(k) * NV * PL + v * PL + o]; };
 
