@@ -79,7 +79,9 @@ __device__ __forceinline__ double sqrt_nr(double x) {
 //                +-inf; a smaller argument gives a signed zero (no subnormal
 //                results); NaN stays NaN (quiet).
 // tests/test_gpu_convert.py checks both against IEEE conversions on the host,
-// bit for bit, over random bit patterns and every boundary of the formats.
+// bit for bit, over random bit patterns and every boundary of the formats;
+// tests/test_convert_algorithm.py restates the bit manipulation in numpy and
+// checks it the same way without a GPU.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double widen_f32(float f) {
   const unsigned u = __float_as_uint(f);
