@@ -237,15 +237,16 @@ __device__ __forceinline__ void phase_load(const StageArgs& a, int bxi, int byi,
       const int gi = gi0 - 2 + rx, gj = gj0 - 2 + ry;
       double ps = u[b][PS];
       if (a.stage == 1) ps = glmf * ps;
-      T w[NV], pr, ro;
+      T w[NV];
+      double pr, ro;
       u2v_cell<T, OMHD_FAST>(u[b], f1g, f1g32, ps, w, pr, ro);
 #pragma unroll
       for (int v = 0; v < NV; ++v) W[v * PL + q] = w[v];
       if (cx_in && cy_in && gi <= ix - 2 && gj <= jx - 2) {  // owner check, u2v.f90:36-45
-        if (!pos_<T, OMHD_FAST>(pr))
-          raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, 0, 0, to_f64<T>(pr));
-        else if (!pos_<T, OMHD_FAST>(ro))
-          raise_error(a.err, OMHD_NEG_DENSITY, gi + 1, gj + 1, 0, 0, to_f64<T>(ro));
+        if (!gt0_<OMHD_FAST>(pr))
+          raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, 0, 0, pr);
+        else if (!gt0_<OMHD_FAST>(ro))
+          raise_error(a.err, OMHD_NEG_DENSITY, gi + 1, gj + 1, 0, 0, ro);
       }
     }
   }

@@ -142,15 +142,16 @@ __device__ __forceinline__ void load_plane(const StageArgs& a, T* W, int slot, i
     for (int v = 0; v < NV; ++v) u[v] = U[v * N + c];
     double ps = u[PS];
     if (a.stage == 1) ps = glmf * ps;
-    T w[NV], pr, ro;
+    T w[NV];
+    double pr, ro;
     u2v_cell<T, OMHD_FAST>(u, f1g, f1g32, ps, w, pr, ro);  // 3D_basic/u2v.f90
 #pragma unroll
     for (int v = 0; v < NV; ++v) Ws[v * PL + q] = w[v];
     if (own_plane && cx_in && cy_in && gi <= ix - 2 && gj <= jx - 2) {  // u2v.f90:36-45, owner check
-      if (!(pr > T(0)))
-        raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, gk + 1, 0, to_f64<T>(pr));
-      else if (!(ro > T(0)))
-        raise_error(a.err, OMHD_NEG_DENSITY, gi + 1, gj + 1, gk + 1, 0, to_f64<T>(ro));
+      if (!(pr > 0.0))
+        raise_error(a.err, OMHD_NEG_PRESSURE, gi + 1, gj + 1, gk + 1, 0, pr);
+      else if (!(ro > 0.0))
+        raise_error(a.err, OMHD_NEG_DENSITY, gi + 1, gj + 1, gk + 1, 0, ro);
     }
   }
 }

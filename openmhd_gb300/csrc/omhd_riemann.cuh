@@ -811,7 +811,8 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
 
 // u2v.f90:11-27 for one cell, into the face arithmetic's type: w = (vx, vy,
 // vz, p, rho, Bx, By, Bz, psi) with the given (GLM-scaled) psi; pr and ro
-// return p and rho for the positivity check (u2v.f90:36-45).
+// return p and rho for the positivity check (u2v.f90:36-45), in FP64 as the
+// recovery computed them (binary32 values widened exactly).
 // FP64 kernels: the reference's FP64 recovery.  FP32-mixed kernels: binary32
 // recovery where E >= rho v^2 + B^2, i.e. where the internal energy is at
 // least the kinetic plus the magnetic energy, so that the pressure -- a
@@ -820,7 +821,7 @@ __device__ __forceinline__ void riemann_flux(const T (&L)[NV], const T (&R)[NV],
 // Mach, and every unphysical state, whose check then sees FP64 values).
 template <class T, bool FAST>
 __device__ __forceinline__ void u2v_cell(const double (&u)[NV], double f1g, float f1g32, double psi, T (&w)[NV],
-                                         T& pr, T& ro) {
+                                         double& pr, double& ro) {
   if constexpr (sizeof(T) == 4) {
     const float r = narrow_f64(u[RO]), mx = narrow_f64(u[MX]), my = narrow_f64(u[MY]), mz = narrow_f64(u[MZ]);
     const float bx = narrow_f64(u[BX]), by = narrow_f64(u[BY]), bz = narrow_f64(u[BZ]), en = narrow_f64(u[EN]);
@@ -838,8 +839,8 @@ __device__ __forceinline__ void u2v_cell(const double (&u)[NV], double f1g, floa
       w[BY] = by;
       w[BZ] = bz;
       w[PS] = narrow_f64(psi);
-      pr = w[PR];
-      ro = r;
+      pr = widen_f32(w[PR]);
+      ro = widen_f32(r);
       return;
     }
   }
@@ -861,17 +862,8 @@ __device__ __forceinline__ void u2v_cell(const double (&u)[NV], double f1g, floa
   w[BY] = to_face<T>(by);
   w[BZ] = to_face<T>(bz);
   w[PS] = to_face<T>(psi);
-  pr = sizeof(T) == 8 ? T(p) : w[PR];
-  ro = sizeof(T) == 8 ? T(r) : w[RO];
-}
-
-// x > 0, false for NaN (the IEEE compare; FP64 on the integer pipe in FAST builds)
-template <class T, bool FAST>
-__device__ __forceinline__ bool pos_(T x) {
-  if constexpr (sizeof(T) == 8)
-    return gt0_<FAST>(x);
-  else
-    return x > T(0);
+  pr = p;
+  ro = r;
 }
 
 // Fast magnetosonic speed used by set_dt (2D_basic/set_dt.f90:27-34).
