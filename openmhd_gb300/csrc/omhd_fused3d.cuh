@@ -32,6 +32,9 @@ namespace d3 {
 #ifndef OMHD_3D_TILE_Y
 #define OMHD_3D_TILE_Y 8
 #endif
+#ifndef OMHD_3D_MIXED_MIN_CTAS  // resident CTAs per SM the FP32-mixed 3D kernel is built for
+#define OMHD_3D_MIXED_MIN_CTAS 2
+#endif
 constexpr int TX = OMHD_3D_TILE_X, TY = OMHD_3D_TILE_Y, NT = TX * TY;
 static_assert(TY * NV <= NT - TX, "the x and y wall fixes use disjoint threads");
 constexpr int RX = TX + 4, RY = TY + 4, PL = RX * RY;  // plane of the halo tile
@@ -160,7 +163,7 @@ __device__ __forceinline__ void load_plane(const StageArgs& a, T* W, int slot, i
 // shared memory each), so that one CTA's FP64 loads, updates and barriers
 // overlap the other's face work.
 template <class T, int FLUX>
-__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 2 : 1) k_stage3d(const StageArgs a) {
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? OMHD_3D_MIXED_MIN_CTAS : 1) k_stage3d(const StageArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* W = reinterpret_cast<T*>(smem_raw);  // [NRING][NV][PL]
   T* SLx = W + NRING * NV * PL;  // [NV][NXS3]; x fluxes in place
