@@ -361,9 +361,9 @@ int omhd_ensemble_sync(omhd_ensemble* e, omhd_step_info* infos);
  * step record back and waits for the stream before it returns, and a failure
  * the kernels record (negative pressure or density, dt too small) is returned
  * with its cell and value in omhd_last_error().  Every call reuses the same
- * array: calls that overlap on the GPU race.  The first call on a device
- * (with it current) looks up the array's device address and SM count, so it
- * should come before any stream capture.
+ * array: calls that overlap on the GPU race.  Because every call copies the
+ * step record to host memory and waits for its stream, no call may be made
+ * while its stream is being captured into a CUDA graph.
  * ==================================================================== */
 int omhd_step2d_noalloc(double* U_dev, const omhd_config* cfg, double t0, int nsteps, void* stream,
                         omhd_step_info* info);
