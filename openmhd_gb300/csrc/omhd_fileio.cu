@@ -101,8 +101,8 @@ int omhd_fileio_output(const char* path, int nd, int ix, int jx, int kx, double 
 
 int omhd_fileio_input(const char* path, int nd, int ix, int jx, int kx, double* t, double* x, double* y, double* z,
                       double* U) {
-  if (!path || !t || !x || !y || !U || (nd != 2 && nd != 3)) return OMHD_BAD_ARG;
-  if (nd == 3 && !z) return OMHD_BAD_ARG;
+  if (!path || !t || !x || !y || !U || (nd != 2 && nd != 3) || ix < 1 || jx < 1) return OMHD_BAD_ARG;
+  if (nd == 3 && (!z || kx < 1)) return OMHD_BAD_ARG;
   if (nd == 2) kx = 1;
   FILE* f = fopen(path, "rb");
   if (!f) return OMHD_IO_ERR;

@@ -66,6 +66,45 @@ def test_input_rejects_other_sizes(lib, tmp_path):
     assert e.value.code == 4  # OMHD_BAD_ARG, fileio.f90:77-82 "parameter mismatch"
 
 
+def test_wrong_shapes_and_types_are_refused_before_the_library(lib, tmp_path):
+    """The library trusts ix/jx/kx: coordinates, V or U that are smaller than
+    the sizes U implies, or of another type, are refused in Python, and the C
+    entry point refuses sizes below 1, before anything is read or written."""
+    import ctypes as C
+
+    import torch
+
+    from openmhd_gb300 import fileio
+    from openmhd_gb300.solver import OMHD_BAD_ARG
+
+    U = random_state((6, 7), 3)
+    path = tmp_path / "f.dat"
+    x, y = np.zeros(7), np.zeros(6)
+    bad = [
+        dict(x=np.zeros(6), y=y, U=U),
+        dict(x=x, y=np.zeros(5), U=U),
+        dict(x=x, y=y, U=U, V=np.zeros((4, 6, 6))),
+        dict(x=x, y=y, U=U[:8]),
+        dict(x=x, y=y, U=random_state((5, 6, 7), 4)),  # 3D without z
+        dict(x=x, y=y, U=random_state((5, 6, 7), 4), z=np.zeros(4)),
+    ]
+    for kw in bad:
+        with pytest.raises(ValueError):
+            fileio.write(path, 0.0, kw.pop("x"), kw.pop("y"), kw.pop("U"), **kw)
+    with pytest.raises(TypeError):
+        fileio.write(path, 0.0, x, y, torch.from_numpy(U).float())
+    assert not path.exists()
+    for sizes in ((2, 0, 6), (3, 7, 6, 0), (4, 7, 6)):
+        with pytest.raises(ValueError):
+            fileio.read(path, *sizes)
+    t = C.c_double()
+    buf = np.zeros(9 * 7 * 6)
+    for nd, ix, jx, kx in ((2, 7, 0, 1), (3, 7, 6, 0), (3, -1, 6, 5)):
+        st = lib.omhd_fileio_input(str(path).encode(), nd, ix, jx, kx, C.byref(t), buf.ctypes.data,
+                                   buf.ctypes.data, buf.ctypes.data, buf.ctypes.data)
+        assert st == OMHD_BAD_ARG, (nd, ix, jx, kx)
+
+
 def test_input_reports_missing_and_truncated_files(lib, tmp_path):
     """A missing file and a file cut short in its header, coordinates or planes
     are reported as OMHD_IO_ERR (the reference's read would stop)."""
