@@ -31,6 +31,21 @@ from .solver import OmhdError, SolverConfig
 NV = 9
 
 
+def _check_device_array(name: str, a, shape) -> None:
+    """Refuse what the adjoint kernels cannot take as it is: they read and
+    write tuple(shape) float64 values at the tensor's address on the current
+    device, so a smaller, strided, other-typed or other-device tensor is an
+    error here, not an out-of-bounds access on the GPU."""
+    if not isinstance(a, torch.Tensor) or not a.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if a.device.index != torch.cuda.current_device():
+        raise ValueError(f"{name} is on cuda:{a.device.index}, not the current device cuda:{torch.cuda.current_device()}")
+    if a.dtype != torch.float64 or not a.is_contiguous():
+        raise TypeError(f"{name} must be a contiguous float64 tensor")
+    if tuple(a.shape) != tuple(shape):
+        raise ValueError(f"{name} has shape {tuple(a.shape)}, expected {tuple(shape)}")
+
+
 class AdjointRun:
     def __init__(self, cfg: SolverConfig, nsteps: int, checkpoint_every: int | None = None, stream=None):
         if not torch.cuda.is_available():
@@ -104,6 +119,9 @@ class AdjointRun:
 
     def step_vjp(self, Un, U1, log3, lam_in, lam_out):
         """Adjoint of one step given its stage inputs (device tensors); lam_in is overwritten."""
+        for name, a, shape in (("Un", Un, self.cfg.shape), ("U1", U1, self.cfg.shape), ("log3", log3, (3,)),
+                               ("lam_in", lam_in, self.cfg.shape), ("lam_out", lam_out, self.cfg.shape)):
+            _check_device_array(name, a, shape)
         self._check(self.lib.omhd_adjoint_step_vjp(self._h, Un.data_ptr(), U1.data_ptr(), log3.data_ptr(),
                                                    lam_in.data_ptr(), lam_out.data_ptr()), "step adjoint failed")
 

@@ -175,3 +175,16 @@ def test_routine_wrappers_refuse_undersized_arrays(lib):
         routines.facefix(np.zeros((9, 6, 7)), np.zeros((9, 6, 8)), 1)
     with pytest.raises(ValueError, match="one entry per domain side"):
         routines.bc(U, kind=(0, 0, 0, 0))
+
+
+def test_step_vjp_arrays_are_checked_on_the_host():
+    """The adjoint step's stage inputs are refused in Python unless they are
+    contiguous float64 CUDA tensors of the state's shape ({dt, ch, glm} for
+    log3): here, without a GPU, every CPU tensor is refused with TypeError."""
+    import torch
+
+    from openmhd_gb300.adjoint import _check_device_array
+
+    for a in (torch.zeros(9, 6, 7, dtype=torch.float64), torch.zeros(3), [0.0, 0.0, 0.0]):
+        with pytest.raises(TypeError):
+            _check_device_array("Un", a, (9, 6, 7))

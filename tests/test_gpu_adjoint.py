@@ -233,3 +233,25 @@ def test_memory_report(cuda_lib):
     assert run.memory_bytes >= S * (10 + 20 + 10) + 3 * 100 * 8 + tape
     assert run.memory_bytes < S * (10 + 20 + 10) + 3 * 100 * 8 + tape + 4096
     assert math.isfinite(run.memory_bytes)
+
+
+def test_step_vjp_refuses_wrong_arrays_before_any_launch(cuda_lib):
+    """A smaller, other-typed or strided stage input, or a log3 of other than
+    three values, is refused in Python; nothing reaches the kernels."""
+    from openmhd_gb300.adjoint import AdjointRun
+
+    cfg = small_cfg("periodic_mc", 26, 20)
+    run = AdjointRun(cfg, 2, 1)
+    good = lambda: torch.zeros(cfg.shape, dtype=torch.float64, device="cuda")  # noqa: E731
+    log3 = torch.zeros(3, dtype=torch.float64, device="cuda")
+    small = torch.zeros((9, cfg.jx - 1, cfg.ix), dtype=torch.float64, device="cuda")
+    strided = torch.zeros((9, cfg.ix, cfg.jx), dtype=torch.float64, device="cuda").transpose(1, 2)
+    with pytest.raises(ValueError):
+        run.step_vjp(good(), good(), log3, good(), small)
+    with pytest.raises(ValueError):
+        run.step_vjp(good(), good(), log3[:2], good(), good())
+    with pytest.raises(TypeError):
+        run.step_vjp(good().float(), good(), log3, good(), good())
+    with pytest.raises(TypeError):
+        run.step_vjp(good(), strided, log3, good(), good())
+    torch.cuda.synchronize()
