@@ -67,6 +67,8 @@ class Ensemble:
     def init_models(self, models: list[ModelSpec]):
         import torch
 
+        if len(models) != len(self.cfgs):  # the library reads one model per member
+            raise ValueError(f"{len(models)} models for {len(self.cfgs)} members")
         torch.cuda.current_stream().synchronize()
         arr = (_lib.Model * len(models))(*[m.to_c() for m in models])
         st = self.lib.omhd_ensemble_init_models(self._h, arr)
@@ -107,8 +109,12 @@ class Ensemble:
         return list(infos)
 
     def member_state(self, i: int) -> np.ndarray:
+        if not 0 <= i < len(self.cfgs):
+            raise IndexError(f"member {i} of {len(self.cfgs)}")
         h = C.c_void_p()
-        self.lib.omhd_ensemble_member(self._h, i, C.byref(h))
+        st = self.lib.omhd_ensemble_member(self._h, i, C.byref(h))
+        if st:
+            raise OmhdError(st, f"no member {i}")
         out = np.empty(self.cfgs[i].shape)
         st = self.lib.omhd_solver_get_state(h, out.ctypes.data)
         if st:

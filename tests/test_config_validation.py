@@ -188,3 +188,18 @@ def test_step_vjp_arrays_are_checked_on_the_host():
     for a in (torch.zeros(9, 6, 7, dtype=torch.float64), torch.zeros(3), [0.0, 0.0, 0.0]):
         with pytest.raises(TypeError):
             _check_device_array("Un", a, (9, 6, 7))
+
+
+def test_ensemble_model_count_and_member_index_are_checked_on_the_host():
+    """One model per member and member indices in range, refused before the
+    library reads a model array or a member handle."""
+    from openmhd_gb300.ensemble import Ensemble, batched_problem_set
+
+    cfgs, models = batched_problem_set(4, seed=1)
+    ens = Ensemble.__new__(Ensemble)  # the checks run before any GPU work
+    ens.cfgs, ens._h = cfgs, None
+    with pytest.raises(ValueError):
+        ens.init_models(models[:3])
+    for i in (-1, 4):
+        with pytest.raises(IndexError):
+            ens.member_state(i)
