@@ -35,6 +35,15 @@ sys.path.insert(0, ROOT)
 
 NX, NY = 4096, 2048
 WORKLOAD = "kh2d_4096x2048_hlld_minmod_glm_tvdrk2"
+
+
+def headline_config(ws: int) -> dict:
+    """The workload both arms (this library and the reference) run, in the same
+    words: KH 4096x2048, HLLD + minmod + GLM + TVD-RK2, CFL 0.4, FP64."""
+    return {"workload": WORKLOAD, "nx": NX, "ny": NY, "precision": "fp64", "cfl": 0.4,
+            "l2": "state 605 MB > 129 MB L2: no flush needed", "parallelism": f"replicas{ws}"}
+
+
 # Algorithmic cost of one 2D cell-update (both RK stages, GLM, CFL) is read
 # from profiles/flops_kh2d.txt (flop-counting build of the oracle on this
 # workload: add/sub/mul/div/sqrt/exp = 1 flop, min/max/abs/sign/compare = 0).
@@ -330,9 +339,9 @@ def run_reference(args):
         "impl": "reference", "metric": "cell-updates/s", "value": base["value"], "unit": "cell-updates/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "precision": "fp64",
-                   "note": "reference is Fortran (no compiler here or on the box): its own source translated "
-                           "mechanically to C (oracle/ref.py), OpenMP; else the C restatement"},
+        "config": headline_config(ws),
+        "note": "the reference is Fortran (no compiler here or on the box): its own source translated "
+                "mechanically to C (oracle/ref.py), OpenMP, timed on rank 0; else the C restatement",
         "cpu_baseline": base,
         "e2e": {"value": base["value"], "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -484,8 +493,7 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_fp64 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded KH initial state)",
-        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "precision": "fp64", "cfl": 0.4,
-                   "l2": "state 605 MB > 129 MB L2: no flush needed", "parallelism": f"replicas{ws}"},
+        "config": headline_config(ws),
         "roofline": roofline,
         "gpu_launches": 2 * args.steps,
         "max_div_b": div_b,

@@ -43,6 +43,8 @@ def test_reference_arm_line(small_baseline, capsys, monkeypatch):
     assert (line["n_gpus"], line["steps"], line["warmup"]) == (1, 2, 3)
     assert line["scaling"] == "weak" and line["vs_baseline"] is None and line["dtype"] == "f64"
     assert line["config"]["workload"] == small_baseline.WORKLOAD
+    # the same config dict as the GPU arm's line, key for key
+    assert line["config"] == small_baseline.headline_config(1)
     cb = line["cpu_baseline"]
     assert cb["kind"] == small_baseline.kind_expected and cb["cores"] == 1 and cb["value"] == line["value"]
     assert "64x32" in cb["sample"]
