@@ -847,7 +847,7 @@ def run_adjoint(args, ndir: int = 16, eps: float = 1e-6):
                  "samples": samples}
     return {
         "workload": f"kh2d_{ADJ_NX}x{ADJ_NY}_fp64_{ADJ_STEPS}steps_adjoint_J=sum(By^2)_d/dvy0",
-        "steps": ADJ_STEPS, "checkpoint_every": ADJ_EVERY, "J": float(J),
+        "steps": ADJ_STEPS, "checkpoint_every": ADJ_EVERY, "J": float(J.detach()),
         "forward_s": t_fwd, "forward_with_checkpoints_s": t_fwd_ck, "backward_s": t_bwd,
         "backward_over_forward": t_bwd / t_fwd,
         "adjoint_step_ms": 1e3 * t_vjp, "forward_step_ms": 1e3 * t_step,
