@@ -5,7 +5,7 @@ from identical initial states.
 * Kelvin-Helmholtz 4096x2048 (HLLD, minmod, GLM, TVD-RK2, zero-gradient y
   walls, CFL 0.4): the headline workload of the benchmark.  1 step within 1e-12
   and 10 steps within 1e-9 per variable, in the scaled L1 norm and in each
-  variable's own relative L1 norm (the benchmark spec's tolerances for the FP64 path).
+  variable's own relative L1 norm (the FP64 path's parity tolerances).
 * Orszag-Tang 256x256 (HLLD, MC, GLM, periodic) run to t = pi, the reference
   2D_basic problem: the same step count as the reference loop (which stops at
   the first t >= tend, main.f90:73) and all 9 fields within the N-step tolerance.
