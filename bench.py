@@ -155,6 +155,7 @@ def _errors(a, b):
             "linf": dict(zip(VAR_NAMES, map(float, li))),
             "max_scaled_l1": float(sc.max()),
             "max_own_norm_rel_l1_significant": float(own[sig].max()) if sig.any() else 0.0,
+            "max_own_norm_var": VAR_NAMES[int(np.argmax(np.where(sig, own, -1.0)))] if sig.any() else None,
             "significant_vars": [v for v, g in zip(VAR_NAMES, sig) if g]}
 
 
@@ -539,6 +540,14 @@ def run_ours(args):
     return 0
 
 
+def _member_summary(i: int, own_vars: list, cfgs: list, models: list) -> dict:
+    """Which ensemble member, model, grid (with ghosts) and variable an error
+    figure belongs to."""
+    return {"member": i, "var": own_vars[i],
+            "model": {0: "orszag_tang", 1: "kelvin_helmholtz"}.get(models[i].kind, str(models[i].kind)),
+            "ix": cfgs[i].ix, "jx": cfgs[i].jx}
+
+
 def run_batched(args, fp64_peak: float = float("nan"), fp32_peak: float = float("nan")):
     """128-member ensemble (seeded sizes in {128..1024}^2, half OT, half KH),
     FP32-mixed, one persistent batched kernel per RK stage, autotuned tiling,
@@ -589,7 +598,7 @@ def run_batched(args, fp64_peak: float = float("nan"), fp32_peak: float = float(
     updates64 = sum(n * (a.steps - b.steps) for n, a, b in zip(cells_m, ref.sync(), before64))
     ref.step(total_steps - 3 - args.steps)
     ref.sync()
-    errs, owns, lis = [], [], []
+    errs, owns, own_vars, lis = [], [], [], []
     low = cnt = 0.0
     for i in range(len(cfgs)):
         Ui = ens.member_state(i)[:, 1:-1, 1:-1]
@@ -598,6 +607,7 @@ def run_batched(args, fp64_peak: float = float("nan"), fp32_peak: float = float(
         e = _errors(Ui, ref.member_state(i)[:, 1:-1, 1:-1])
         errs.append(e["max_scaled_l1"])
         owns.append(e["max_own_norm_rel_l1_significant"])
+        own_vars.append(e["max_own_norm_var"])
         lis.append(max(e["linf"].values()))
     del ref
     batch_share = low / max(cnt, 1.0)
@@ -610,6 +620,7 @@ def run_batched(args, fp64_peak: float = float("nan"), fp32_peak: float = float(
             "max_member_own_norm_rel_l1_vs_fp64": max(owns),
             "median_member_own_norm_rel_l1_vs_fp64": float(np.median(owns)),
             "members_own_norm_within_1e-6": int(sum(o <= 1e-6 for o in owns)),
+            "worst_member_own_norm": _member_summary(int(np.argmax(owns)), own_vars, cfgs, models),
             "members_scaled_within_1e-6": int(sum(x <= 1e-6 for x in errs)),
             "max_member_linf_vs_fp64": max(lis),
             "members_stepping_throughout": active,

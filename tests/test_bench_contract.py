@@ -104,3 +104,26 @@ def test_u2v_fp64_share_follows_the_energy_test():
     U[3] = [1.0, 1.0, 0.9, 1.0]      # E: cell 1 has E = rho v^2, cell 2 E < B^2
     assert bench._u2v_fp64_share([U]) == 0.25
     assert bench._u2v_fp64_share([U[:, :2], U[:, 2:]]) == 0.25
+
+
+def test_error_report_names_the_worst_significant_variable():
+    """_errors picks the largest own-norm error among the variables that hold at
+    least 1e-4 of their physical scale, and names it; _member_summary names the
+    ensemble member's model and grid."""
+    import numpy as np
+
+    import bench
+    from openmhd_gb300.ensemble import batched_problem_set
+
+    rng = np.random.default_rng(0)
+    b = rng.uniform(0.5, 1.5, (9, 8, 8))
+    b[2] *= 1e-9  # mz: below 1e-4 of the momentum scale, not significant
+    a = b.copy()
+    a[2] += 1e-9  # a large own-norm error in an insignificant variable is not the max
+    a[6] += 1e-8
+    e = bench._errors(a, b)
+    assert "mz" not in e["significant_vars"] and e["max_own_norm_var"] == "by"
+    assert e["max_own_norm_rel_l1_significant"] == e["own_norm_rel_l1"]["by"]
+    cfgs, models = batched_problem_set(4, seed=0)
+    s = bench._member_summary(1, ["ro", "by", "en", "mx"], cfgs, models)
+    assert s == {"member": 1, "var": "by", "model": "kelvin_helmholtz", "ix": cfgs[1].ix, "jx": cfgs[1].jx}
